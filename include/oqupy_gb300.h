@@ -1,0 +1,121 @@
+/*
+ * oqupy_gb300 -- C ABI of the GB300 TEMPO / PT-TEMPO / process-tensor engine.
+ *
+ * Plain pointers and sizes only.  Complex numbers are complex128 stored as
+ * interleaved (re, im) doubles.  Matrices are row-major.  Every function
+ * returns an otb_status (0 = OK, < 0 = error; otb_last_error() has the text).
+ *
+ * Ownership: host input buffers are read during the call only (copied to the
+ * device).  The library owns the device memory of a handle until
+ * *_destroy.  Outputs go to caller-allocated host buffers.
+ * Threading: a handle is not thread-safe; distinct handles may be used from
+ * distinct threads/streams.  `stream` is a cudaStream_t (NULL = default).
+ *
+ * Reference interfaces replaced (OQuPy 0.5.0, paths relative to the project):
+ *   otb_tempo_*  -> oqupy/backends/tempo_backend.py:577-626
+ *                   (TempoBackend.__init__/initialize/compute_step), batched
+ *   otb_pt_*     -> oqupy/backends/pt_tempo_backend.py:56-316
+ *                   (PtTempoBackend.__init__/initialize/compute_step/
+ *                    get_mpo_tensor/update_process_tensor)
+ *   otb_dyn_*    -> oqupy/system_dynamics.py:41-182, 631-700
+ *                   (compute_dynamics hot loop over a process tensor)
+ */
+#ifndef OQUPY_GB300_H
+#define OQUPY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t otb_status;
+
+#define OTB_OK 0
+#define OTB_ERR_INVALID_ARG (-1)
+#define OTB_ERR_OOM (-2)
+#define OTB_ERR_CUDA (-3)
+#define OTB_ERR_NO_CONVERGENCE (-4)
+#define OTB_ERR_TIMEOUT (-5)
+#define OTB_ERR_NONFINITE (-6)
+#define OTB_ERR_CHI_OVERFLOW (-7)
+
+#define OTB_PRECISION_COMPLEX128 0
+/* FP32 site tensors, contractions and Jacobi rotations; FP64 column norms,
+ * tail sums, rank decisions, log-norm and read-out accumulation. */
+#define OTB_PRECISION_MIXED 1
+
+/* ------------------------------------------------------------------ TEMPO */
+
+typedef struct otb_tempo otb_tempo;
+
+typedef struct {
+  int32_t precision;   /* OTB_PRECISION_* */
+  int32_t chi_cap;     /* bond-dimension capacity of every site (<= 128) */
+  int32_t out_cap;     /* states kept per instance (ring), >= 2 */
+  int32_t grid;        /* CTAs per launch, 0 = 2 per SM */
+} otb_tempo_config;
+
+typedef struct {
+  int32_t hs_dim;             /* d; Liouville dimension D = d*d (<= 9) */
+  int32_t dkmax;              /* memory length; < 0 = full memory (grows) */
+  double epsrel;              /* relative SVD truncation tolerance */
+  int32_t n_influences;       /* influence matrices given (dk = 0..n-1) */
+  const double* influences;   /* n_influences * D * D complex, [dk][a][r],
+                                 coupling eigenbasis; dk=0 is diagonal */
+  const double* prop1;        /* D*D: first half-step, eigenbasis-folded  */
+  const double* prop2;        /* D*D: second half-step, eigenbasis-folded */
+  const double* rho0;         /* D: vectorised initial state */
+  int32_t max_sites;          /* site-slot hint (full memory), 0 = auto */
+} otb_tempo_instance;
+
+typedef struct {
+  int32_t step;       /* completed steps */
+  int32_t status;     /* 0 or a negative otb_status */
+  int32_t nsites;     /* MPS sites incl. the trailing propagator node */
+  int32_t max_bond;   /* largest bond dimension after the last step */
+  double log_scale;   /* log of the norm factored out (mixed precision) */
+} otb_tempo_info;
+
+/* Replaces TempoBackend.__init__ + initialize (tempo_backend.py:583-617). */
+otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n_instances,
+                            const otb_tempo_instance* instances,
+                            otb_tempo** out);
+void otb_tempo_destroy(otb_tempo* h);
+/* Replaces nsteps calls of TempoBackend.compute_step (tempo_backend.py:619-626)
+ * for every instance of the handle. */
+otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stream);
+/* States of steps [first_step, first_step+count) of one instance, each D
+ * complex; steps must still be held by the output ring (step 0 = rho0). */
+otb_status otb_tempo_read_states(otb_tempo* h, int32_t inst, int32_t first_step,
+                                 int32_t count, double* out);
+/* All instances, steps [first_step, first_step+count): out[inst][k][D]. */
+otb_status otb_tempo_read_all_states(otb_tempo* h, int32_t first_step,
+                                     int32_t count, double* out);
+otb_status otb_tempo_get_info(otb_tempo* h, int32_t inst, otb_tempo_info* info);
+/* Bond dimensions of the current MPS (sites - 1 values); returns the count
+ * through *count. */
+otb_status otb_tempo_bond_dims(otb_tempo* h, int32_t inst, int32_t* out,
+                               int32_t cap, int32_t* count);
+/* Influence matrix for one dk (grows storage; full-memory runs append one
+ * per step, tempo_backend.py:487-497). */
+otb_status otb_tempo_set_influence(otb_tempo* h, int32_t inst, int32_t dk,
+                                   const double* mat);
+/* Propagators for the next step (time-dependent systems, tempo.py:400-435). */
+otb_status otb_tempo_set_propagators(otb_tempo* h, int32_t inst,
+                                     const double* prop1, const double* prop2);
+/* Influence replacing the oldest window site in the next step only
+ * (add_correlation_time, tempo_backend.py:503-517). */
+otb_status otb_tempo_set_first_influence(otb_tempo* h, int32_t inst,
+                                         const double* mat);
+/* Grow the site ring of every instance to at least nslots slots. */
+otb_status otb_tempo_reserve_sites(otb_tempo* h, int32_t nslots);
+
+const char* otb_last_error(void);
+int32_t otb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OQUPY_GB300_H */

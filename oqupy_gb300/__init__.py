@@ -1,0 +1,12 @@
+"""GB300-native backend for OQuPy's TEMPO / PT-TEMPO / process-tensor path.
+
+The compute path is ``liboqupy_gb300.so`` (hand-written sm_103a CUDA, C ABI in
+``include/oqupy_gb300.h``).  This package is the host side: the batched API
+(``TempoBatch``), the drop-in backends that ``oqupy.Tempo`` / ``oqupy.PtTempo``
+select through ``backend_config={"backend": "gb300", ...}`` once
+``install()`` has run, and a device process tensor for ``compute_dynamics``.
+"""
+
+from .tempo import TempoBatch, GpuTempoBackend, fold_propagators  # noqa: F401
+
+__all__ = ["TempoBatch", "GpuTempoBackend", "fold_propagators"]

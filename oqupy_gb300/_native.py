@@ -1,0 +1,135 @@
+"""ctypes binding of ``liboqupy_gb300.so`` (declared in include/oqupy_gb300.h).
+
+The library is the only compute path of this package: if it cannot be
+loaded, every entry point raises.  There is no CPU fallback.
+"""
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboqupy_gb300.so")
+
+OTB_OK = 0
+OTB_ERR_INVALID_ARG = -1
+OTB_ERR_OOM = -2
+OTB_ERR_CUDA = -3
+OTB_ERR_NO_CONVERGENCE = -4
+OTB_ERR_TIMEOUT = -5
+OTB_ERR_NONFINITE = -6
+OTB_ERR_CHI_OVERFLOW = -7
+
+PRECISION = {"complex128": 0, "mixed": 1}
+
+STATUS_TEXT = {
+    OTB_ERR_INVALID_ARG: "invalid argument",
+    OTB_ERR_OOM: "out of device memory",
+    OTB_ERR_CUDA: "CUDA error",
+    OTB_ERR_NO_CONVERGENCE: "Jacobi SVD did not converge",
+    OTB_ERR_TIMEOUT: "device wait timed out",
+    OTB_ERR_NONFINITE: "non-finite values in a bond split",
+    OTB_ERR_CHI_OVERFLOW: "bond dimension exceeded chi_cap",
+}
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+
+
+class TempoConfig(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("chi_cap", ctypes.c_int32),
+                ("out_cap", ctypes.c_int32), ("grid", ctypes.c_int32)]
+
+
+class TempoInstance(ctypes.Structure):
+    _fields_ = [("hs_dim", ctypes.c_int32), ("dkmax", ctypes.c_int32),
+                ("epsrel", ctypes.c_double), ("n_influences", ctypes.c_int32),
+                ("influences", c_double_p), ("prop1", c_double_p),
+                ("prop2", c_double_p), ("rho0", c_double_p),
+                ("max_sites", ctypes.c_int32)]
+
+
+class TempoInfo(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("nsites", ctypes.c_int32), ("max_bond", ctypes.c_int32),
+                ("log_scale", ctypes.c_double)]
+
+
+class DeviceError(RuntimeError):
+    """A status code returned by the CUDA library."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_TEXT.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def _declare(lib):
+    P = ctypes.c_void_p
+    i32 = ctypes.c_int32
+    sig = {
+        "otb_tempo_create": (i32, [ctypes.POINTER(TempoConfig), i32,
+                                   ctypes.POINTER(TempoInstance), ctypes.POINTER(P)]),
+        "otb_tempo_destroy": (None, [P]),
+        "otb_tempo_advance": (i32, [P, i32, P]),
+        "otb_tempo_read_states": (i32, [P, i32, i32, i32, c_double_p]),
+        "otb_tempo_read_all_states": (i32, [P, i32, i32, c_double_p]),
+        "otb_tempo_get_info": (i32, [P, i32, ctypes.POINTER(TempoInfo)]),
+        "otb_tempo_bond_dims": (i32, [P, i32, c_int32_p, i32, c_int32_p]),
+        "otb_tempo_set_influence": (i32, [P, i32, i32, c_double_p]),
+        "otb_tempo_set_propagators": (i32, [P, i32, c_double_p, c_double_p]),
+        "otb_tempo_set_first_influence": (i32, [P, i32, c_double_p]),
+        "otb_tempo_reserve_sites": (i32, [P, i32]),
+        "otb_last_error": (ctypes.c_char_p, []),
+        "otb_version": (i32, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return sig
+
+
+def exported_symbols():
+    """Names the header declares and this binding calls."""
+    return [
+        "otb_tempo_create", "otb_tempo_destroy", "otb_tempo_advance",
+        "otb_tempo_read_states", "otb_tempo_read_all_states",
+        "otb_tempo_get_info", "otb_tempo_bond_dims", "otb_tempo_set_influence",
+        "otb_tempo_set_propagators", "otb_tempo_set_first_influence",
+        "otb_tempo_reserve_sites", "otb_last_error", "otb_version"]
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: run oqupy_gb300.build.build() first "
+                "(the GPU path has no CPU fallback)")
+        l = ctypes.CDLL(LIB_PATH)
+        _declare(l)
+        _lib = l
+    return _lib
+
+
+def check(code: int):
+    if code != OTB_OK:
+        msg = lib().otb_last_error().decode(errors="replace")
+        raise DeviceError(code, msg)
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(c_double_p)
+
+
+def cplx(a) -> np.ndarray:
+    """complex array -> contiguous interleaved float64 view."""
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+    return a.view(np.float64).reshape(a.shape + (2,))

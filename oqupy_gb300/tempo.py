@@ -1,0 +1,266 @@
+"""Batched TEMPO on the GPU and the drop-in ``TempoBackend`` replacement.
+
+``TempoBatch`` advances many independent TEMPO instances (different
+couplings, temperatures, memory lengths and bond dimensions) in one CUDA
+launch per call.  ``GpuTempoBackend`` has the constructor and methods of the
+reference's ``TempoBackend`` (oqupy/backends/tempo_backend.py:577-626) and
+runs one instance through the same C ABI, so ``oqupy.Tempo`` can use it
+unchanged (see ``oqupy_gb300.install``).
+"""
+
+import ctypes
+from copy import copy
+from typing import Callable, Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _native as nat
+
+DEFAULT_CHI_CAP = 64
+
+
+def super_unitaries(unitary: np.ndarray):
+    """``(super_u, super_u_dagg)`` of tempo_backend.py:383-388:
+    ``left_right_super(U, U^dag)`` and ``left_right_super(U^dag, U)``
+    (operators.py:149-153, ``kron(left, right.T)``)."""
+    u = np.asarray(unitary, dtype=np.complex128)
+    ud = u.conjugate().T
+    return np.kron(u, ud.T), np.kron(ud, u.T)
+
+
+def fold_propagators(prop1, prop2, unitary=None):
+    """Fold the coupling-eigenbasis rotation that the reference attaches to
+    the dk=0 influence tensor (tempo_backend.py:419-424) into the half-step
+    propagators: ``P1 <- super_u_dagg P1`` and ``P2 <- P2 super_u``.  The
+    engine then works with diagonal dk=0 influences only."""
+    p1 = np.asarray(prop1, dtype=np.complex128)
+    p2 = np.asarray(prop2, dtype=np.complex128)
+    if unitary is None or np.allclose(unitary, np.identity(len(unitary))):
+        return p1, p2
+    su, sud = super_unitaries(unitary)
+    return sud @ p1, p2 @ su
+
+
+class TempoBatch:
+    """Many TEMPO instances advanced together on the GPU.
+
+    Parameters
+    ----------
+    instances: sequence of dicts with keys
+        ``hs_dim`` (d), ``dkmax`` (int, or None for full memory),
+        ``epsrel``, ``influences`` (array ``[n, D, D]``, dk = 0..n-1, in the
+        coupling eigenbasis; ``influence_matrix`` output of the reference),
+        ``prop1``, ``prop2`` (``D x D`` half-step propagators),
+        ``rho0`` (``d x d`` or ``D``), optional ``unitary`` (coupling
+        eigenvectors; folded into the propagators).
+    precision: ``"complex128"`` or ``"mixed"``.
+    chi_cap: bond-dimension capacity of every site slot.
+    out_cap: number of recent states kept per instance on the device.
+    """
+
+    def __init__(self, instances: Sequence[Dict], precision: str = "complex128",
+                 chi_cap: int = DEFAULT_CHI_CAP, out_cap: int = 2, grid: int = 0,
+                 max_sites: int = 0):
+        L = nat.lib()
+        if precision not in nat.PRECISION:
+            raise ValueError(f"precision must be one of {list(nat.PRECISION)}")
+        self.precision = precision
+        self.n = len(instances)
+        if self.n == 0:
+            raise ValueError("need at least one instance")
+        self._keep = []
+        arr = (nat.TempoInstance * self.n)()
+        self.D = []
+        for i, inst in enumerate(instances):
+            d = int(inst["hs_dim"])
+            D = d * d
+            infl = nat.cplx(np.asarray(inst["influences"]).reshape(-1, D, D))
+            p1, p2 = fold_propagators(inst["prop1"], inst["prop2"],
+                                      inst.get("unitary"))
+            p1, p2 = nat.cplx(p1), nat.cplx(p2)
+            rho0 = nat.cplx(np.asarray(inst["rho0"]).reshape(D))
+            self._keep += [infl, p1, p2, rho0]
+            dk = inst.get("dkmax")
+            arr[i].hs_dim = d
+            arr[i].dkmax = -1 if dk is None else int(dk)
+            arr[i].epsrel = float(inst["epsrel"])
+            arr[i].n_influences = infl.shape[0]
+            arr[i].influences = nat.dptr(infl)
+            arr[i].prop1 = nat.dptr(p1)
+            arr[i].prop2 = nat.dptr(p2)
+            arr[i].rho0 = nat.dptr(rho0)
+            arr[i].max_sites = int(max_sites)
+            self.D.append(D)
+        cfg = nat.TempoConfig(nat.PRECISION[precision], int(chi_cap),
+                              int(out_cap), int(grid))
+        self.out_cap = int(out_cap)
+        self.chi_cap = int(chi_cap)
+        h = ctypes.c_void_p()
+        nat.check(L.otb_tempo_create(ctypes.byref(cfg), self.n, arr, ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            nat.lib().otb_tempo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stepping --------------------------------------------------------
+    def advance(self, nsteps: int = 1, stream: Optional[int] = None):
+        """Advance every instance by ``nsteps`` TEMPO steps (asynchronous
+        on ``stream``; status is checked when results are read)."""
+        nat.check(nat.lib().otb_tempo_advance(self._h, int(nsteps),
+                                               ctypes.c_void_p(stream or 0)))
+
+    def info(self, i: int) -> Dict:
+        inf = nat.TempoInfo()
+        nat.check(nat.lib().otb_tempo_get_info(self._h, int(i), ctypes.byref(inf)))
+        return {"step": inf.step, "status": inf.status, "nsites": inf.nsites,
+                "max_bond": inf.max_bond, "log_scale": inf.log_scale}
+
+    def check_status(self):
+        for i in range(self.n):
+            st = self.info(i)["status"]
+            if st != 0:
+                raise nat.DeviceError(st, f"instance {i}")
+
+    def states(self, first: int = 0, count: Optional[int] = None) -> np.ndarray:
+        """States of steps ``[first, first+count)`` for all instances as a
+        complex array ``[n, count, D]`` (uniform D) or a list."""
+        if count is None:
+            count = self.info(0)["step"] + 1 - first
+        if len(set(self.D)) == 1:
+            out = np.zeros((self.n, count, self.D[0], 2))
+            nat.check(nat.lib().otb_tempo_read_all_states(
+                self._h, int(first), int(count), nat.dptr(out)))
+            return out.view(np.complex128)[..., 0]
+        res = []
+        for i in range(self.n):
+            res.append(self.instance_states(i, first, count))
+        return res
+
+    def instance_states(self, i: int, first: int, count: int) -> np.ndarray:
+        out = np.zeros((count, self.D[i], 2))
+        nat.check(nat.lib().otb_tempo_read_states(self._h, int(i), int(first),
+                                                  int(count), nat.dptr(out)))
+        return out.view(np.complex128)[..., 0]
+
+    def bond_dims(self, i: int) -> List[int]:
+        buf = (ctypes.c_int32 * 4096)()
+        cnt = ctypes.c_int32()
+        nat.check(nat.lib().otb_tempo_bond_dims(self._h, int(i), buf, 4096,
+                                                ctypes.byref(cnt)))
+        return list(buf[:cnt.value])
+
+    # -- per-step inputs (drop-in backend) ---------------------------------
+    def set_influence(self, i: int, dk: int, mat):
+        m = nat.cplx(mat)
+        nat.check(nat.lib().otb_tempo_set_influence(self._h, int(i), int(dk), nat.dptr(m)))
+
+    def set_propagators(self, i: int, p1, p2, unitary=None):
+        a, b = fold_propagators(p1, p2, unitary)
+        a, b = nat.cplx(a), nat.cplx(b)
+        nat.check(nat.lib().otb_tempo_set_propagators(self._h, int(i), nat.dptr(a), nat.dptr(b)))
+
+    def set_first_influence(self, i: int, mat=None):
+        if mat is None:
+            nat.check(nat.lib().otb_tempo_set_first_influence(self._h, int(i), None))
+        else:
+            m = nat.cplx(mat)
+            nat.check(nat.lib().otb_tempo_set_first_influence(self._h, int(i), nat.dptr(m)))
+
+    def reserve_sites(self, nslots: int):
+        nat.check(nat.lib().otb_tempo_reserve_sites(self._h, int(nslots)))
+
+
+class GpuTempoBackend:
+    """Drop-in for ``oqupy.backends.tempo_backend.TempoBackend``
+    (tempo_backend.py:577-626): same constructor, ``step`` property,
+    ``initialize() -> (0, state)`` and ``compute_step() -> (step, state)``.
+
+    ``config`` keys used: ``precision`` ("complex128" | "mixed"), ``chi_cap``.
+    Degeneracy maps (``unique=True``) are not supported by the GPU engine;
+    ``oqupy_gb300.install`` routes such runs to the reference backend.
+    """
+
+    def __init__(self, initial_state, influence: Callable[[int], np.ndarray],
+                 unitary_transform, propagators, sum_north, sum_west, dkmax,
+                 epsrel, config: Optional[Dict] = None, degeneracy_maps=None,
+                 dim=None):
+        if degeneracy_maps is not None:
+            raise NotImplementedError("the GPU TEMPO engine needs unique=False")
+        if not (np.allclose(sum_north, 1.0) and np.allclose(sum_west, 1.0)):
+            raise NotImplementedError("the GPU TEMPO engine needs all-ones sums")
+        self._initial_state = np.array(initial_state, dtype=np.complex128).reshape(-1)
+        self._influence = influence
+        self._unitary = np.asarray(unitary_transform, dtype=np.complex128)
+        self._propagators = propagators
+        self._dkmax = dkmax
+        self._epsrel = epsrel
+        self._config = {} if config is None else config
+        self._step = None
+        self._batch: Optional[TempoBatch] = None
+        self._last_props = None
+        self._ninfl = 0
+
+    @property
+    def step(self):
+        return self._step
+
+    def initialize(self):
+        D = self._initial_state.size
+        d = int(round(np.sqrt(D)))
+        n = 1 if self._dkmax is None else self._dkmax + 1
+        infl = np.array([self._influence(dk) for dk in range(n)],
+                        dtype=np.complex128)
+        p1, p2 = self._propagators(0)
+        self._last_props = (np.array(p1), np.array(p2))
+        inst = dict(hs_dim=d, dkmax=self._dkmax, epsrel=self._epsrel,
+                    influences=infl, prop1=p1, prop2=p2,
+                    rho0=self._initial_state, unitary=self._unitary)
+        self._batch = TempoBatch(
+            [inst], precision=self._config.get("precision", "complex128"),
+            chi_cap=int(self._config.get("chi_cap", DEFAULT_CHI_CAP)),
+            out_cap=4, grid=1, max_sites=16 if self._dkmax is None else 0)
+        self._ninfl = n
+        self._step = 0
+        return self._step, copy(self._initial_state)
+
+    def compute_step(self):
+        b = self._batch
+        step = self._step + 1
+        p1, p2 = self._propagators(step - 1)
+        if not (np.array_equal(p1, self._last_props[0])
+                and np.array_equal(p2, self._last_props[1])):
+            b.set_propagators(0, p1, p2, self._unitary)
+            self._last_props = (np.array(p1), np.array(p2))
+        if self._dkmax is None:
+            # the window of step s holds dk = 0 .. s-1 (tempo_backend.py:487-497)
+            while self._ninfl < step:
+                b.set_influence(0, self._ninfl, self._influence(self._ninfl))
+                self._ninfl += 1
+            need = step + 2
+            if b.info(0)["nsites"] + 2 > getattr(self, "_slots", 16):
+                self._slots = max(2 * getattr(self, "_slots", 16), need)
+                b.reserve_sites(self._slots)
+        elif step > self._dkmax:
+            neg = self._influence(self._dkmax - step)
+            if neg is not None:
+                b.set_first_influence(0, neg)
+        b.advance(1)
+        inf = b.info(0)
+        if inf["status"] != 0:
+            raise nat.DeviceError(inf["status"], f"TEMPO step {step}")
+        state = b.instance_states(0, step, 1)[0]
+        self._step = step
+        return self._step, state
+
+    def bond_dimensions(self) -> List[int]:
+        return self._batch.bond_dims(0)
