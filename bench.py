@@ -1,0 +1,361 @@
+"""Benchmark: batched spin-boson TEMPO trajectories/sec on one GB300.
+
+Workload (the batched TEMPO configuration): 512 spin-boson instances, seeded:
+alpha ~ U[0.01, 0.5], omega_c ~ U[1, 10], T ~ U[0, 5], ohmic exponential
+cutoff, H = Omega/2 sigma_x with Omega ~ U[0.5, 2], bath operator sigma_z/2,
+dkmax ~ U{20..300}, dt = 0.05, epsrel = 1e-6, 500 steps per trajectory,
+rho0 = spin up.  Inputs are synthetic (seeded draws of those distributions).
+
+One bench step = one TEMPO time step of every instance (one kernel launch).
+``value`` = instances x timed steps / 500 / timed seconds, i.e. whole
+trajectories per second at the cost of the timed steps; the per-step cost
+grows with the memory window (min(step, dkmax+1) sites), so the timed window
+is stated in ``config``.  The headline form is "mixed" (double-float Jacobi on
+the FP32 pipe, FP64 everything else); the complex128 form runs the same steps
+and the trace distance between the two is reported.
+
+``--impl reference`` times the CPU oracle (a plain-numpy restatement of the
+reference TEMPO backend) on the same workload and steps, on all host cores.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+NSTEPS_TRAJ = 500
+METRIC = "spin-boson trajectories/sec on 1 GB300, mixed vs complex128, at 1e-6 trace dist"
+
+
+def make_instances(n, seed):
+    import numpy as np
+    from oqupy_gb300 import bath
+    rng = np.random.default_rng(seed)
+    sx = np.array([[0, 1], [1, 0]], dtype=complex)
+    sz = np.diag([1.0, -1.0]).astype(complex)
+    out = []
+    for _ in range(n):
+        a = rng.uniform(0.01, 0.5)
+        wc = rng.uniform(1.0, 10.0)
+        T = rng.uniform(0.0, 5.0)
+        om = rng.uniform(0.5, 2.0)
+        dk = int(rng.integers(20, 301))
+        infl, U = bath.influences(a, 1.0, wc, "exponential", T, 0.05, dk, 0.5 * sz)
+        p1, p2 = bath.half_step_propagators(0.5 * om * sx, 0.05)
+        out.append(dict(hs_dim=2, dkmax=dk, epsrel=1e-6, influences=infl,
+                        prop1=p1, prop2=p2,
+                        rho0=np.diag([1.0, 0.0]).astype(complex), unitary=U,
+                        params=(a, wc, T, om)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (reference arm / cpu_baseline)
+# ---------------------------------------------------------------------------
+
+def _oracle_worker(args):
+    """Run one instance through the oracle: W untimed steps, K timed steps."""
+    inst, warm, steps = args
+    import numpy as np
+    from oracle import tempo_oracle as to
+    infl = inst["influences"]
+    p1, p2 = inst["prop1"], inst["prop2"]
+    D = 4
+    o = to.TempoOracle(inst["rho0"].reshape(-1), lambda dk: infl[dk],
+                       inst["unitary"], lambda s: (p1, p2), np.ones(D),
+                       np.ones(D), inst["dkmax"], inst["epsrel"])
+    o.initialize()
+    for _ in range(warm):
+        o.compute_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.compute_step()
+    return time.perf_counter() - t0
+
+
+def cpu_oracle_rate(insts, warm, steps, procs):
+    """Trajectories/sec of the oracle on ``insts`` (timed steps only) with
+    ``procs`` single-threaded worker processes."""
+    import multiprocessing as mp
+    env_keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    old = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = "1"
+    try:
+        ctx = mp.get_context("spawn")
+        t0 = time.perf_counter()
+        with ctx.Pool(procs) as pool:
+            per = pool.map(_oracle_worker, [(i, warm, steps) for i in insts])
+        wall = time.perf_counter() - t0
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    cpu_seconds = float(sum(per))
+    # instances run concurrently on `procs` cores: whole-machine throughput
+    rate = len(insts) * steps / NSTEPS_TRAJ / (cpu_seconds / procs)
+    return rate, cpu_seconds, wall
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def trace_distance_max(a, b):
+    import numpy as np
+    d = (a - b).reshape(a.shape[:-1] + (2, 2))
+    h = 0.5 * (d + np.conj(np.swapaxes(d, -1, -2)))
+    ev = np.linalg.eigvalsh(h)
+    return 0.5 * np.abs(ev).sum(axis=-1)
+
+
+def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64):
+    from oqupy_gb300 import TempoBatch
+    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap,
+                   out_cap=warm + steps + 1)
+    stream = torch.cuda.current_stream()
+    for _ in range(warm):
+        b.advance(1, stream.cuda_stream)
+    torch.cuda.synchronize()
+    b.check_status()
+    f0 = sum(b.info(i)["flops_alg"] for i in range(b.n))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()                       # evict L2 between timed steps
+        ev[k][0].record(stream)
+        b.advance(1, stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    b.check_status()
+    infos = [b.info(i) for i in range(b.n)]
+    flops = sum(x["flops_alg"] for x in infos) - f0
+    states = b.states(0, warm + steps + 1)
+    stats = {"max_bond": max(x["max_bond"] for x in infos),
+             "splits": sum(x["splits"] for x in infos),
+             "sweeps64_per_split": sum(x["sweeps64"] for x in infos) / max(1, sum(x["splits"] for x in infos)),
+             "sweepsff_per_split": sum(x["sweeps32"] for x in infos) / max(1, sum(x["splits"] for x in infos))}
+    b.close()
+    return sum(ms), ms, flops, states, stats
+
+
+def run_e2e(torch, insts, precision, warm, steps, chi_cap=64):
+    """End to end through the public API: host inputs -> device (create),
+    all steps, states -> host; returns (seconds, h2d bytes, d2h bytes)."""
+    import numpy as np
+    from oqupy_gb300 import TempoBatch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + steps + 1)
+    b.advance(warm + steps)
+    st = b.states(0, warm + steps + 1)
+    t1 = time.perf_counter()
+    b.close()
+    h2d = sum(i["influences"].nbytes + 2 * i["prop1"].nbytes + i["rho0"].nbytes for i in insts)
+    return t1 - t0, int(h2d), int(st.nbytes)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--cpu-sample", type=int, default=512)
+    ap.add_argument("--no-complex128", action="store_true")
+    ap.add_argument("--chi-cap", type=int, default=64)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    seed = 20261203 + rank
+
+    workload = {"workload": "batched TEMPO spin-boson, 512 instances (alpha U[0.01,0.5], "
+                            "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, "
+                            "dt 0.05, epsrel 1e-6, 500-step trajectories)",
+                "instances_per_gpu": args.instances,
+                "timed_steps": f"{args.warmup + 1}..{args.warmup + args.steps} of {NSTEPS_TRAJ}",
+                "l2": "flushed (256 MiB write) before every timed step",
+                "seed": seed}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        insts = make_instances(args.instances, seed)
+        procs = os.cpu_count() or 1
+        rate, cpu_s, wall = cpu_oracle_rate(insts, args.warmup, args.steps, procs)
+        per_step_ms = cpu_s / procs / args.steps * 1e3
+        line = {"metric": METRIC, "value": rate, "unit": "trajectories/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "c128", "data": "synthetic", "config": workload, "impl": "reference",
+                "cpu_baseline": {"value": rate, "unit": "trajectories/s", "cores": procs,
+                                 "kind": "port",
+                                 "sample": f"{len(insts)} instances x steps {args.warmup + 1}.."
+                                           f"{args.warmup + args.steps}, numpy oracle, one "
+                                           f"single-threaded process per core"},
+                "e2e": {"value": rate, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import numpy as np
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from oqupy_gb300 import _native
+    insts = make_instances(args.instances, seed)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler()
+    barrier()
+    clocks.start()
+    t_mixed, ms_mixed, fl_mixed, st_mixed, stats_mixed = run_gpu_form(
+        torch, insts, "mixed", args.warmup, args.steps, flush, args.chi_cap)
+    clk = clocks.stop()
+    barrier()
+    t_mixed_s = t_mixed / 1e3
+    if world > 1:
+        t = torch.tensor([t_mixed_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_mixed_s = float(t.item())
+    value = world * args.instances * args.steps / NSTEPS_TRAJ / t_mixed_s
+
+    res = {}
+    if not args.no_complex128:
+        t_c, ms_c, fl_c, st_c, stats_c = run_gpu_form(torch, insts, "complex128",
+                                                       args.warmup, args.steps, flush,
+                                                       args.chi_cap)
+        td = trace_distance_max(st_mixed, st_c).max(axis=1)
+        res = {"complex128_value": world * args.instances * args.steps / NSTEPS_TRAJ / (t_c / 1e3),
+               "complex128_ms_per_step": t_c / args.steps,
+               "mixed_speedup_vs_complex128": t_c / t_mixed,
+               "mixed_vs_complex128_trace_distance": {
+                   "max": float(td.max()), "median": float(np.median(td)),
+                   "frac_le_1e-6": float(np.mean(td <= 1e-6))},
+               "complex128_stats": stats_c}
+
+    e2e_s, h2d, d2h = run_e2e(torch, insts, "mixed", args.warmup, args.steps, args.chi_cap)
+    e2e_steps = args.warmup + args.steps
+    e2e = {"value": world * args.instances * e2e_steps / NSTEPS_TRAJ / e2e_s,
+           "unit": "trajectories/s", "h2d_bytes_per_step": h2d // e2e_steps,
+           "d2h_bytes_per_step": d2h // e2e_steps,
+           "note": "fresh handle: host inputs uploaded, steps 1..W+K, all states read back"}
+
+    peak_fp32 = _native.fma_peak_tflops(1)
+    peak_fp64 = _native.fma_peak_tflops(0)
+    achieved = fl_mixed / t_mixed_s / 1e12
+    roofline = {"bound": "fp32-pipe", "achieved": achieved, "peak": peak_fp32,
+                "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
+                "kernel": "tempo_kernel<true> (double-float Jacobi)",
+                "achieved_def": "algorithmic flops (complex R-SVD count per split + contractions) / event time",
+                "peak_source": "measured FFMA throughput (otb_measure_fma_peak)",
+                "fp64_pipe_peak_tflops": peak_fp64}
+    if res:
+        ach_c = fl_c / (t_c / 1e3) / 1e12
+        roofline["complex128"] = {"bound": "fp64-pipe", "achieved": ach_c, "peak": peak_fp64,
+                                  "frac": ach_c / peak_fp64}
+    prof = os.path.join(ROOT, "profiles", "tempo_kernel_traffic.json")
+    if os.path.exists(prof):
+        try:
+            roofline["traffic"] = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            pass
+
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_sample > 0:
+        procs = os.cpu_count() or 1
+        sample = insts[: args.cpu_sample]
+        rate, cpu_s, wall = cpu_oracle_rate(sample, args.warmup, args.steps, procs)
+        cpu = {"value": rate, "unit": "trajectories/s", "cores": procs, "kind": "port",
+               "sample": f"{len(sample)} instances x steps {args.warmup + 1}..{args.warmup + args.steps}"
+                         f" ({cpu_s:.1f} CPU-s), numpy oracle, one process per core"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "trajectories/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (Jacobi in double-float)",
+                "data": "synthetic", "config": dict(workload, precision="mixed",
+                                                    parallelism=f"instances x {world} GPUs"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk, "gpu_launches": args.steps, "mixed_stats": stats_mixed}
+        line.update(res)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -41,8 +41,10 @@ typedef int32_t otb_status;
 #define OTB_ERR_CHI_OVERFLOW (-7)
 
 #define OTB_PRECISION_COMPLEX128 0
-/* FP32 site tensors, contractions and Jacobi rotations; FP64 column norms,
- * tail sums, rank decisions, log-norm and read-out accumulation. */
+/* Bond splits: FP32 one-sided Jacobi (rotations accumulated in FP32) as a
+ * preconditioner, then B = A V in FP64 and FP64 Jacobi sweeps to
+ * convergence; site tensors, contractions, norms, rank decisions and the
+ * read-out stay FP64. */
 #define OTB_PRECISION_MIXED 1
 
 /* ------------------------------------------------------------------ TEMPO */
@@ -74,7 +76,13 @@ typedef struct {
   int32_t status;     /* 0 or a negative otb_status */
   int32_t nsites;     /* MPS sites incl. the trailing propagator node */
   int32_t max_bond;   /* largest bond dimension after the last step */
-  double log_scale;   /* log of the norm factored out (mixed precision) */
+  double log_scale;   /* log of a norm factored out of the MPS (0 here) */
+  int32_t splits;     /* truncated SVD splits done so far */
+  int32_t sweeps64;   /* FP64 Jacobi sweeps done so far */
+  int32_t sweeps32;   /* double-float Jacobi sweeps done so far (mixed) */
+  double flops_alg;   /* algorithmic flops done so far: per split of a complex
+                         R x N matrix (R >= N) 4 (6 R N^2 + 20 N^3), plus
+                         8 flops per complex multiply-add of the contractions */
 } otb_tempo_info;
 
 /* Replaces TempoBackend.__init__ + initialize (tempo_backend.py:583-617). */
@@ -110,6 +118,11 @@ otb_status otb_tempo_set_first_influence(otb_tempo* h, int32_t inst,
                                          const double* mat);
 /* Grow the site ring of every instance to at least nslots slots. */
 otb_status otb_tempo_reserve_sites(otb_tempo* h, int32_t nslots);
+
+/* Measured FMA-pipe throughput of this GPU (TFLOP/s, 2 flops per FMA):
+ * precision 0 = FP64 (DFMA), 1 = FP32 (FFMA).  Used as the roofline peak of
+ * the Jacobi kernels, which run on these pipes. */
+otb_status otb_measure_fma_peak(int32_t precision, double* tflops);
 
 const char* otb_last_error(void);
 int32_t otb_version(void);

@@ -54,7 +54,9 @@ class TempoInstance(ctypes.Structure):
 class TempoInfo(ctypes.Structure):
     _fields_ = [("step", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("nsites", ctypes.c_int32), ("max_bond", ctypes.c_int32),
-                ("log_scale", ctypes.c_double)]
+                ("log_scale", ctypes.c_double), ("splits", ctypes.c_int32),
+                ("sweeps64", ctypes.c_int32), ("sweeps32", ctypes.c_int32),
+                ("flops_alg", ctypes.c_double)]
 
 
 class DeviceError(RuntimeError):
@@ -84,6 +86,7 @@ def _declare(lib):
         "otb_tempo_set_propagators": (i32, [P, i32, c_double_p, c_double_p]),
         "otb_tempo_set_first_influence": (i32, [P, i32, c_double_p]),
         "otb_tempo_reserve_sites": (i32, [P, i32]),
+        "otb_measure_fma_peak": (i32, [i32, c_double_p]),
         "otb_last_error": (ctypes.c_char_p, []),
         "otb_version": (i32, []),
     }
@@ -101,7 +104,15 @@ def exported_symbols():
         "otb_tempo_read_states", "otb_tempo_read_all_states",
         "otb_tempo_get_info", "otb_tempo_bond_dims", "otb_tempo_set_influence",
         "otb_tempo_set_propagators", "otb_tempo_set_first_influence",
-        "otb_tempo_reserve_sites", "otb_last_error", "otb_version"]
+        "otb_tempo_reserve_sites", "otb_measure_fma_peak", "otb_last_error",
+        "otb_version"]
+
+
+def fma_peak_tflops(precision: int) -> float:
+    """Measured FMA-pipe peak of the current GPU (0 = FP64, 1 = FP32)."""
+    v = ctypes.c_double()
+    check(lib().otb_measure_fma_peak(int(precision), ctypes.byref(v)))
+    return v.value
 
 
 def lib() -> ctypes.CDLL:

@@ -21,7 +21,7 @@ struct otb_tempo {
   int grid = 0;
   int block = 256;
   int Dmax = 0;
-  size_t elem = 16;  // bytes per site element
+  size_t elem = 16;  // bytes per site element (complex128 in both forms)
   std::vector<InstDev> inst;
   std::vector<InstState> state;  // host shadow (refreshed on demand)
   std::vector<int> order;
@@ -141,7 +141,7 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   h->precision = cfg->precision;
   h->cap = cfg->chi_cap;
   h->out_cap = cfg->out_cap;
-  h->elem = cfg->precision == 0 ? 16 : 8;
+  h->elem = 16;
   h->inst.resize(n);
   h->state.resize(n);
   h->infl_host.resize(n);
@@ -187,6 +187,10 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     st.log_scale = 0.0;
     st.max_bond = 1;
     st.ovr_active = 0;
+    st.splits = 0;
+    st.sweeps64 = 0;
+    st.sweeps32 = 0;
+    st.flops_alg = 0.0;
   }
   long long out_total = 0;
   for (int i = 0; i < n; ++i) {
@@ -216,18 +220,10 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     const InstDev& I = h->inst[i];
     const int D = I.D;
     std::vector<double> r0(ins[i].rho0, ins[i].rho0 + 2 * D);
-    if (h->precision == 0) {
-      if (!check_cuda(cudaMemcpy((char*)h->d_sites.p + I.site_base * h->elem, r0.data(),
-                                 r0.size() * sizeof(double), cudaMemcpyHostToDevice),
-                      "init site"))
-        return OTB_ERR_CUDA;
-    } else {
-      std::vector<float> f(r0.begin(), r0.end());
-      if (!check_cuda(cudaMemcpy((char*)h->d_sites.p + I.site_base * h->elem, f.data(),
-                                 f.size() * sizeof(float), cudaMemcpyHostToDevice),
-                      "init site"))
-        return OTB_ERR_CUDA;
-    }
+    if (!check_cuda(cudaMemcpy((char*)h->d_sites.p + I.site_base * h->elem, r0.data(),
+                               r0.size() * sizeof(double), cudaMemcpyHostToDevice),
+                    "init site"))
+      return OTB_ERR_CUDA;
     int2 d0 = make_int2(1, 1);
     if (!check_cuda(cudaMemcpy((int2*)h->d_dims.p + I.dims_base, &d0, sizeof(int2),
                                cudaMemcpyHostToDevice),
@@ -256,8 +252,8 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, 2 * std::max(sms, 1)));
   h->wcap = (long long)(h->cap * h->Dmax) * (h->cap * h->Dmax);
-  h->work_stride = 3 * h->wcap;
-  if (!h->d_work.alloc((size_t)h->grid * h->work_stride * h->elem)) return OTB_ERR_OOM;
+  h->work_stride = tempo_work_bytes(h->wcap);
+  if (!h->d_work.alloc((size_t)h->grid * h->work_stride)) return OTB_ERR_OOM;
   *out = h.release();
   return OTB_OK;
 }
@@ -299,7 +295,7 @@ extern "C" otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stre
   L.queue = (int*)h->d_queue.p;
   L.order = (const int*)h->d_order.p;
   L.nsteps = nsteps;
-  L.smem_elems = 0;
+  L.smem_bytes = 0;
   if (!check_cuda(launch_tempo(L, h->precision, h->grid, h->block, s), "tempo launch"))
     return OTB_ERR_CUDA;
   return OTB_OK;
@@ -319,6 +315,10 @@ extern "C" otb_status otb_tempo_get_info(otb_tempo* h, int32_t inst, otb_tempo_i
   info->nsites = s.nsites;
   info->max_bond = s.max_bond;
   info->log_scale = s.log_scale;
+  info->splits = s.splits;
+  info->sweeps64 = s.sweeps64;
+  info->sweeps32 = s.sweeps32;
+  info->flops_alg = s.flops_alg;
   return OTB_OK;
 }
 
@@ -357,6 +357,12 @@ extern "C" otb_status otb_tempo_read_all_states(otb_tempo* h, int32_t first, int
                   "read state"))
     return OTB_ERR_CUDA;
   size_t off = 0;
+  for (int i = 0; i < h->n; ++i) {
+    if (h->state[i].status != 0)
+      return set_error(h->state[i].status, "instance " + std::to_string(i) + " stopped at step " +
+                                               std::to_string(h->state[i].step) + " with status " +
+                                               std::to_string(h->state[i].status));
+  }
   for (int i = 0; i < h->n; ++i) {
     const InstDev& I = h->inst[i];
     const int step = h->state[i].step;

@@ -32,6 +32,10 @@ struct InstState {
   double log_scale;
   int max_bond;    // largest bond dimension seen in the last step
   int ovr_active;  // 1: use the override influence for the first window site
+  int splits;      // truncated SVD splits done so far
+  int sweeps64;    // FP64 Jacobi sweeps done so far
+  int sweeps32;    // double-float Jacobi sweeps done so far (mixed form)
+  double flops_alg;  // algorithmic flops done so far (R-SVD count + contractions)
 };
 
 struct TempoLaunch {
@@ -39,21 +43,26 @@ struct TempoLaunch {
   const InstDev* inst;
   InstState* state;
   int2* dims;                // (l, r) per slot
-  void* sites;               // cx<T> arena
+  void* sites;               // complex128 arena
   const double* infl;        // complex128 interleaved
   const double* props;       // complex128 interleaved
   double* out;               // complex128 interleaved
-  void* work;                // per-CTA workspace (cx<T>)
-  long long work_stride;     // elements of cx<T> per CTA in `work`
-  long long wcap;            // elements of one matrix buffer in the workspace
+  void* work;                // per-CTA workspace (bytes)
+  long long work_stride;     // bytes per CTA in `work`
+  long long wcap;            // complex elements of one matrix buffer
   int* queue;                // work-queue counter (reset before each launch)
   const int* order;          // instance processing order
   int nsteps;                // steps to advance
-  int smem_elems;            // cx<T> capacity of the dynamic shared buffer
+  int smem_bytes;            // capacity of the dynamic shared buffer
 };
 
-// precision: 0 = complex128, 1 = mixed (FP32 sites/contractions/Jacobi,
-// FP64 norms, tail sums, rank decisions and read-out accumulation)
+// Per-CTA workspace: three FP64 complex matrices of wcap elements (W, theta
+// copy / temporaries, carry) and one double-float complex one (mixed form).
+inline long long tempo_work_bytes(long long wcap) { return wcap * (3 * 16 + 16); }
+
+// precision: 0 = complex128 (FP64 Jacobi), 1 = mixed (double-float Jacobi
+// on the FP32 pipe; FP64 sites, contractions, rotation angles, norms, rank
+// decisions and read-out)
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
                          cudaStream_t stream);
 int tempo_smem_bytes(int precision);

@@ -1,0 +1,73 @@
+// Double-float ("FF") arithmetic: a value is the unevaluated sum hi + lo of
+// two floats (about 48 significant bits).  Built from the classical
+// error-free transformations (Knuth two-sum, Dekker fast-two-sum, FMA-based
+// two-product).  Used by the mixed-precision Jacobi so that its rotations run
+// on the FP32 pipe at close to FP64 accuracy.
+#pragma once
+
+#include "common.cuh"
+
+namespace otb {
+
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_make(float h, float l) {
+  ff r;
+  r.hi = h;
+  r.lo = l;
+  return r;
+}
+__device__ __forceinline__ ff ff_from(double d) {
+  const float h = (float)d;
+  return ff_make(h, (float)(d - (double)h));
+}
+__device__ __forceinline__ double ff_to(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Knuth: s + e == a + b exactly
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return ff_make(s, e);
+}
+// Dekker, |a| >= |b|
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return ff_make(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = two_sum(a.hi, b.hi);
+  const float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_make(-b.hi, -b.lo)); }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+// acc + a * b
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff acc) { return ff_add(acc, ff_mul(a, b)); }
+
+__device__ __forceinline__ ff ff_shfl_xor(ff v, int off) {
+  return ff_make(__shfl_xor_sync(0xffffffffu, v.hi, off, 32), __shfl_xor_sync(0xffffffffu, v.lo, off, 32));
+}
+
+// complex double-float
+struct cff {
+  ff x, y;
+};
+
+__device__ __forceinline__ cff cff_from(cx<double> z) {
+  cff r;
+  r.x = ff_from(z.x);
+  r.y = ff_from(z.y);
+  return r;
+}
+__device__ __forceinline__ cx<double> cff_to(cff z) { return mk<double>(ff_to(z.x), ff_to(z.y)); }
+
+}  // namespace otb

@@ -13,21 +13,32 @@
 // each round rotates n/2 disjoint column pairs concurrently.  A pair is owned
 // by a group of G lanes (G = 8, 16 or 32 by row count); the three inner
 // products are reduced with xor shuffles inside the group.  Column norms,
-// the descending sort, the tail sums and the rank decision are always done in
-// FP64, also when the matrix itself is FP32.
+// the descending sort, the tail sums and the rank decision are always FP64.
+//
+// Two drivers:
+//  * complex128: FP64 sweeps on the matrix until no pair rotates;
+//  * mixed: FP32 sweeps on an FP32 copy with the rotations accumulated in an
+//    FP32 V, then B = A V formed in FP64 and FP64 sweeps on B, which start
+//    from nearly orthogonal columns and converge in a few sweeps.
 #pragma once
 
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace otb {
 
 constexpr int JACOBI_MAX_SWEEPS = 60;
 
 struct JacobiShared {
+  double red[33];
   int flag[2];
   int kept;
   int status;
+  int sweeps;     // FP64 sweeps of the last split
+  int sweeps32;   // FP32 sweeps of the last split (mixed form)
 };
+
+__device__ __forceinline__ int jacobi_group(int rows) { return rows > 128 ? 32 : (rows > 32 ? 16 : 8); }
 
 template <typename T>
 __device__ __forceinline__ T group_sum(T v, int G) {
@@ -35,102 +46,277 @@ __device__ __forceinline__ T group_sum(T v, int G) {
   return v;
 }
 
-// Orthogonalise the columns of W (m x n, column-major, leading dimension ld)
-// in place: on return W = A V with mutually orthogonal columns.  Afterwards
-// norm[j] = ||W_j||_2 (FP64), perm[0..n) lists the columns by descending
-// norm, and the return value is the kept rank (>= 1).  Must be called by all
-// threads of the CTA.  norm/perm must hold n entries (shared memory).
+// Sweeps of one-sided Jacobi on W (m x n, column-major, leading dim ld).
+// With V != nullptr the same rotations are applied to V (n x n, ld ldv).
+// Returns the number of sweeps done (JACOBI_MAX_SWEEPS = not converged).
+//
+// Numerical-zero floor: a column whose squared norm is below
+// (16 sqrt(m) eps)^2 times the largest squared column norm holds only
+// rounding noise of the other columns; pairs involving such a column are not
+// rotated (rotating noise against a real column regenerates noise at the
+// stopping threshold and never converges).  The floor changes nothing above
+// the rounding level of the decomposition.
 template <typename T>
-__device__ int jacobi_truncate(cx<T>* W, int m, int n, int ld, double epsrel, double* norm,
-                               int* perm, JacobiShared* sh) {
+__device__ int jacobi_sweeps(cx<T>* W, int m, int n, int ld, cx<T>* V, int ldv, JacobiShared* sh,
+                             int max_sweeps = JACOBI_MAX_SWEEPS, T tol_scale = (T)1) {
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
-  const int G = (m > 32) ? 32 : ((m > 16) ? 16 : 8);
+  const int G = jacobi_group(m);
   const int lane = tid & (G - 1);
   const int group = tid / G;
   const int ngroups = nthreads / G;
   const int np = (n + 1) >> 1;
   const int nn = np << 1;
-  const T tol = sqrt((T)m) * num<T>::eps();
+  const T tol = tol_scale * sqrt((T)m) * num<T>::eps();
   const T bigz = num<T>::big_zeta();
-
-  if (tid == 0) {
-    sh->flag[0] = 0;
-    sh->status = ST_OK;
-  }
+  if (tid == 0) sh->flag[0] = 0;
   __syncthreads();
-  int sweep = 0;
-  if (n > 1) {
-    for (sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
-      for (int round = 0; round < nn - 1; ++round) {
-        for (int pb = 0; pb < np; pb += ngroups) {
-          const int p = pb + group;
-          int a, b;
-          if (p == 0) {
-            a = nn - 1;
-            b = round;
-          } else {
-            a = (round + p) % (nn - 1);
-            b = (round - p + nn - 1) % (nn - 1);
+  if (n <= 1) return 0;
+  int sweep;
+  for (sweep = 0; sweep < max_sweeps; ++sweep) {
+    T zfloor;
+    {
+      // largest squared column norm (a lower bound of s_max^2)
+      double mx = 0.0;
+      for (int j = tid / 32; j < n; j += nthreads / 32) {
+        const int l = tid & 31;
+        double acc = 0.0;
+        const cx<T>* c = W + (size_t)j * ld;
+        for (int r = l; r < m; r += 32) {
+          const double x = (double)c[r].x, y = (double)c[r].y;
+          acc = fma(x, x, fma(y, y, acc));
+        }
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        mx = fmax(mx, acc);
+      }
+      for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
+      __syncthreads();
+      if (tid == 0) {
+        double v = 0.0;
+        for (int w = 0; w < nthreads / 32; ++w) v = fmax(v, sh->red[w]);
+        sh->red[32] = v;
+      }
+      __syncthreads();
+      const double zf = 16.0 * sqrt((double)m) * (double)num<T>::eps();
+      zfloor = (T)(zf * zf * sh->red[32]);
+    }
+    for (int round = 0; round < nn - 1; ++round) {
+      for (int pb = 0; pb < np; pb += ngroups) {
+        const int p = pb + group;
+        int a, b;
+        if (p == 0) {
+          a = nn - 1;
+          b = round;
+        } else {
+          a = (round + p) % (nn - 1);
+          b = (round - p + nn - 1) % (nn - 1);
+        }
+        if (a > b) {
+          const int t = a;
+          a = b;
+          b = t;
+        }
+        const bool active = (p < np) && (b < n);
+        T al = 0, be = 0, gr = 0, gi = 0;
+        cx<T>* ca = W + (size_t)a * ld;
+        cx<T>* cb = W + (size_t)b * ld;
+        if (active) {
+          for (int r = lane; r < m; r += G) {
+            const cx<T> u = ca[r];
+            const cx<T> v = cb[r];
+            al = fma(u.x, u.x, fma(u.y, u.y, al));
+            be = fma(v.x, v.x, fma(v.y, v.y, be));
+            gr = fma(u.x, v.x, fma(u.y, v.y, gr));
+            gi = fma(u.x, v.y, fma(-u.y, v.x, gi));
           }
-          if (a > b) {
-            const int t = a;
-            a = b;
-            b = t;
-          }
-          const bool active = (p < np) && (b < n);
-          T al = 0, be = 0, gr = 0, gi = 0;
-          cx<T>* ca = W + (size_t)a * ld;
-          cx<T>* cb = W + (size_t)b * ld;
-          if (active) {
+        }
+        al = group_sum(al, G);
+        be = group_sum(be, G);
+        gr = group_sum(gr, G);
+        gi = group_sum(gi, G);
+        if (active) {
+          const T g = sqrt(gr * gr + gi * gi);
+          if (al > zfloor && be > zfloor && g > tol * sqrt(al) * sqrt(be)) {
+            const T zeta = (be - al) / (2 * g);
+            const T az = fabs(zeta);
+            T t = (az > bigz) ? (T)0.5 / az : (T)1 / (az + sqrt((T)1 + zeta * zeta));
+            if (zeta < 0) t = -t;
+            const T c = (T)1 / sqrt((T)1 + t * t);
+            const T s = c * t;
+            const T pr = gr / g, pi = gi / g;  // e^{i phi}
+            // a' = c a - s e^{-i phi} b ;  b' = s e^{i phi} a + c b
             for (int r = lane; r < m; r += G) {
               const cx<T> u = ca[r];
               const cx<T> v = cb[r];
-              al = fma(u.x, u.x, fma(u.y, u.y, al));
-              be = fma(v.x, v.x, fma(v.y, v.y, be));
-              gr = fma(u.x, v.x, fma(u.y, v.y, gr));
-              gi = fma(u.x, v.y, fma(-u.y, v.x, gi));
+              cx<T> nu, nv;
+              nu.x = c * u.x - s * (pr * v.x + pi * v.y);
+              nu.y = c * u.y - s * (pr * v.y - pi * v.x);
+              nv.x = c * v.x + s * (pr * u.x - pi * u.y);
+              nv.y = c * v.y + s * (pr * u.y + pi * u.x);
+              ca[r] = nu;
+              cb[r] = nv;
             }
-          }
-          al = group_sum(al, G);
-          be = group_sum(be, G);
-          gr = group_sum(gr, G);
-          gi = group_sum(gi, G);
-          if (active) {
-            const T g = sqrt(gr * gr + gi * gi);
-            if (al > 0 && be > 0 && g > tol * sqrt(al) * sqrt(be)) {
-              const T zeta = (be - al) / (2 * g);
-              const T az = fabs(zeta);
-              T t = (az > bigz) ? (T)0.5 / az : (T)1 / (az + sqrt((T)1 + zeta * zeta));
-              if (zeta < 0) t = -t;
-              const T c = (T)1 / sqrt((T)1 + t * t);
-              const T s = c * t;
-              const T pr = gr / g, pi = gi / g;  // e^{i phi}
-              // a' = c a - s e^{-i phi} b ;  b' = s e^{i phi} a + c b
-              for (int r = lane; r < m; r += G) {
-                const cx<T> u = ca[r];
-                const cx<T> v = cb[r];
+            if (V != nullptr) {
+              cx<T>* va = V + (size_t)a * ldv;
+              cx<T>* vb = V + (size_t)b * ldv;
+              for (int r = lane; r < n; r += G) {
+                const cx<T> u = va[r];
+                const cx<T> v = vb[r];
                 cx<T> nu, nv;
                 nu.x = c * u.x - s * (pr * v.x + pi * v.y);
                 nu.y = c * u.y - s * (pr * v.y - pi * v.x);
                 nv.x = c * v.x + s * (pr * u.x - pi * u.y);
                 nv.y = c * v.y + s * (pr * u.y + pi * u.x);
-                ca[r] = nu;
-                cb[r] = nv;
+                va[r] = nu;
+                vb[r] = nv;
               }
-              if (lane == 0) sh->flag[sweep & 1] = 1;
             }
+            if (lane == 0) sh->flag[sweep & 1] = 1;
           }
         }
-        __syncthreads();
       }
-      const int rotated = sh->flag[sweep & 1];
-      if (tid == 0) sh->flag[(sweep + 1) & 1] = 0;
       __syncthreads();
-      if (!rotated) break;
     }
+    const int rotated = sh->flag[sweep & 1];
+    if (tid == 0) sh->flag[(sweep + 1) & 1] = 0;
+    __syncthreads();
+    if (!rotated) break;
   }
-  // FP64 column norms
+  return sweep;
+}
+
+// One-sided Jacobi sweeps in double-float arithmetic on W (m x n, ld).
+// Same schedule, stopping test and numerical-zero floor as jacobi_sweeps;
+// the inner products are reduced in FF, the rotation angle is computed in
+// FP64 from them, and the rotation is applied in FF.  Orthogonality reaches
+// about 1e-14 relative, with every per-element operation on the FP32 pipe.
+__device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShared* sh) {
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
+  const int G = jacobi_group(m);
+  const int lane = tid & (G - 1);
+  const int group = tid / G;
+  const int ngroups = nthreads / G;
+  const int np = (n + 1) >> 1;
+  const int nn = np << 1;
+  const double eps_ff = 3.6e-15;  // ~2^-48, double-float unit roundoff
+  const double tol = sqrt((double)m) * eps_ff;
+  if (tid == 0) sh->flag[0] = 0;
+  __syncthreads();
+  if (n <= 1) return 0;
+  int sweep;
+  for (sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
+    double zfloor;
+    {
+      double mx = 0.0;
+      for (int j = tid / 32; j < n; j += nthreads / 32) {
+        const int l = tid & 31;
+        double acc = 0.0;
+        const cff* c = W + (size_t)j * ld;
+        for (int r = l; r < m; r += 32) {
+          const double x = (double)c[r].x.hi, y = (double)c[r].y.hi;
+          acc = fma(x, x, fma(y, y, acc));
+        }
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        mx = fmax(mx, acc);
+      }
+      for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
+      __syncthreads();
+      if (tid == 0) {
+        double v = 0.0;
+        for (int w = 0; w < nthreads / 32; ++w) v = fmax(v, sh->red[w]);
+        sh->red[32] = v;
+      }
+      __syncthreads();
+      const double zf = 16.0 * sqrt((double)m) * eps_ff;
+      zfloor = zf * zf * sh->red[32];
+    }
+    for (int round = 0; round < nn - 1; ++round) {
+      for (int pb = 0; pb < np; pb += ngroups) {
+        const int p = pb + group;
+        int a, b;
+        if (p == 0) {
+          a = nn - 1;
+          b = round;
+        } else {
+          a = (round + p) % (nn - 1);
+          b = (round - p + nn - 1) % (nn - 1);
+        }
+        if (a > b) {
+          const int t = a;
+          a = b;
+          b = t;
+        }
+        const bool active = (p < np) && (b < n);
+        ff al = ff_make(0.f, 0.f), be = al, gr = al, gi = al;
+        cff* ca = W + (size_t)a * ld;
+        cff* cb = W + (size_t)b * ld;
+        if (active) {
+          for (int r = lane; r < m; r += G) {
+            const cff u = ca[r];
+            const cff v = cb[r];
+            al = ff_fma(u.x, u.x, ff_fma(u.y, u.y, al));
+            be = ff_fma(v.x, v.x, ff_fma(v.y, v.y, be));
+            gr = ff_fma(u.x, v.x, ff_fma(u.y, v.y, gr));
+            gi = ff_fma(u.x, v.y, ff_sub(gi, ff_mul(u.y, v.x)));
+          }
+        }
+        for (int off = G >> 1; off > 0; off >>= 1) {
+          al = ff_add(al, ff_shfl_xor(al, off));
+          be = ff_add(be, ff_shfl_xor(be, off));
+          gr = ff_add(gr, ff_shfl_xor(gr, off));
+          gi = ff_add(gi, ff_shfl_xor(gi, off));
+        }
+        if (active) {
+          const double A = ff_to(al), B = ff_to(be), Gr = ff_to(gr), Gi = ff_to(gi);
+          const double g = sqrt(Gr * Gr + Gi * Gi);
+          if (A > zfloor && B > zfloor && g > tol * sqrt(A) * sqrt(B)) {
+            const double zeta = (B - A) / (2 * g);
+            const double az = fabs(zeta);
+            double t = (az > 1e150) ? 0.5 / az : 1.0 / (az + sqrt(1.0 + zeta * zeta));
+            if (zeta < 0) t = -t;
+            const double c = 1.0 / sqrt(1.0 + t * t);
+            const double s = c * t;
+            const double pr = Gr / g, pi = Gi / g;
+            const ff fc = ff_from(c);
+            // q = s e^{-i phi}, w = s e^{i phi}
+            const ff qx = ff_from(s * pr), qy = ff_from(-s * pi);
+            const ff wy = ff_from(s * pi);
+            for (int r = lane; r < m; r += G) {
+              const cff u = ca[r];
+              const cff v = cb[r];
+              cff nu, nv;
+              // nu = c u - q v
+              nu.x = ff_sub(ff_mul(fc, u.x), ff_sub(ff_mul(qx, v.x), ff_mul(qy, v.y)));
+              nu.y = ff_sub(ff_mul(fc, u.y), ff_add(ff_mul(qx, v.y), ff_mul(qy, v.x)));
+              // nv = c v + w u, w = (qx, wy)
+              nv.x = ff_add(ff_mul(fc, v.x), ff_sub(ff_mul(qx, u.x), ff_mul(wy, u.y)));
+              nv.y = ff_add(ff_mul(fc, v.y), ff_add(ff_mul(qx, u.y), ff_mul(wy, u.x)));
+              ca[r] = nu;
+              cb[r] = nv;
+            }
+            if (lane == 0) sh->flag[sweep & 1] = 1;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    const int rotated = sh->flag[sweep & 1];
+    if (tid == 0) sh->flag[(sweep + 1) & 1] = 0;
+    __syncthreads();
+    if (!rotated) break;
+  }
+  return sweep;
+}
+
+// FP64 column norms of W, descending order and the kept rank (>= 1).
+template <typename T>
+__device__ int jacobi_finish(const cx<T>* W, int m, int n, int ld, double epsrel, double* norm,
+                             int* perm, JacobiShared* sh, int sweeps) {
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
   for (int j = tid / 32; j < n; j += nthreads / 32) {
     const int l = tid & 31;
     double acc = 0.0;
@@ -143,7 +329,6 @@ __device__ int jacobi_truncate(cx<T>* W, int m, int n, int ld, double epsrel, do
     if (l == 0) norm[j] = sqrt(acc);
   }
   __syncthreads();
-  // descending order, ties broken by column index
   for (int j = tid; j < n; j += nthreads) {
     const double sj = norm[j];
     int rank = 0;
@@ -167,13 +352,53 @@ __device__ int jacobi_truncate(cx<T>* W, int m, int n, int ld, double epsrel, do
     }
     if (kept < 1) kept = 1;
     sh->kept = kept;
+    sh->sweeps = sweeps;
+    sh->status = ST_OK;
     if (!finite)
       sh->status = ST_NONFINITE;
-    else if (sweep >= JACOBI_MAX_SWEEPS)
+    else if (sweeps >= JACOBI_MAX_SWEEPS)
       sh->status = ST_NO_CONVERGENCE;
   }
   __syncthreads();
   return sh->kept;
+}
+
+// complex128 driver: orthogonalise W (m x n) in place and truncate.
+__device__ inline int jacobi_truncate_fp64(cx<double>* W, int m, int n, int ld, double epsrel,
+                                           double* norm, int* perm, JacobiShared* sh) {
+  const int sw = jacobi_sweeps<double>(W, m, n, ld, nullptr, 0, sh);
+  if (threadIdx.x == 0) sh->sweeps32 = 0;
+  return jacobi_finish<double>(W, m, n, ld, epsrel, norm, perm, sh, sw);
+}
+
+// Mixed driver: W (m x n, FP64, ld m) holds the matrix to split.  It is
+// scaled to unit largest entry, converted to double-float in Wff (m x n),
+// orthogonalised there, and written back (rescaled) to W in FP64, followed by
+// the FP64 finish.  The FF range (float exponent) is why the scaling is done.
+__device__ inline int jacobi_truncate_mixed(cx<double>* W, int m, int n, cff* Wff, double epsrel,
+                                            double* norm, int* perm, JacobiShared* sh) {
+  const int tid = threadIdx.x;
+  const int nt = blockDim.x;
+  double mx = 0.0;
+  for (int idx = tid; idx < m * n; idx += nt) mx = fmax(mx, fmax(fabs(W[idx].x), fabs(W[idx].y)));
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    double v = 0.0;
+    for (int w = 0; w < nt / 32; ++w) v = fmax(v, sh->red[w]);
+    sh->red[32] = (v > 0.0) ? v : 1.0;
+  }
+  __syncthreads();
+  const double scale = sh->red[32];
+  const double inv = 1.0 / scale;
+  for (int idx = tid; idx < m * n; idx += nt) Wff[idx] = cff_from(cscale(W[idx], inv));
+  __syncthreads();
+  const int sw = jacobi_sweeps_ff(Wff, m, n, m, sh);
+  for (int idx = tid; idx < m * n; idx += nt) W[idx] = cscale(cff_to(Wff[idx]), scale);
+  __syncthreads();
+  if (threadIdx.x == 0) sh->sweeps32 = sw;
+  return jacobi_finish<double>(W, m, n, m, epsrel, norm, perm, sh, sw);
 }
 
 }  // namespace otb

@@ -21,10 +21,11 @@
 // is folded into the propagators on the host (P1 <- U_dag P1, P2 <- P2 U_sup),
 // so every influence here is in the coupling eigenbasis.
 //
-// Site tensors live in a per-instance ring of fixed-capacity slots, layout
-// [l][a][r] (row-major).  That layout is also the column-major (a r) x l
-// matrix the right-to-left sweep factorises, so sweep splits need no
-// reshuffle.
+// Site tensors (complex128 in both precision forms) live in a per-instance
+// ring of fixed-capacity slots, layout [l][a][r] (row-major).  That layout is
+// also the column-major (a r) x l matrix the right-to-left sweep factorises,
+// so sweep splits need no reshuffle.  The precision forms differ only in the
+// bond split (jacobi.cuh).
 #include <math.h>
 
 #include "engine.h"
@@ -36,19 +37,20 @@ constexpr int TEMPO_THREADS = 256;
 constexpr int NMAX = 1152;   // max columns of a split (D * cap <= 9 * 128)
 constexpr int VMAX = 128;    // max bond dimension held by the read-out vector (chi_cap <= 128)
 
-template <typename T>
+typedef cx<double> zc;
+
 struct Bufs {
-  cx<T>* sites;
+  zc* sites;
   int2* dims;
-  const cx<double>* infl;
-  const cx<double>* props;
-  cx<double>* out;
-  cx<T>* W;    // working matrix (shared or global)
-  cx<T>* Wg;   // global fallback for W
-  cx<T>* Tg;   // global scratch (theta copy / temporaries)
-  cx<T>* Cg;   // carry S V^H
-  cx<T>* Ws;   // dynamic shared buffer
-  int smem_elems;
+  const zc* infl;
+  const zc* props;
+  zc* out;
+  zc* Wg;            // global working matrix
+  zc* Tg;            // global theta copy / temporaries
+  zc* Cg;            // carry S V^H
+  cff* Wffg;         // global double-float working matrix (mixed form)
+  unsigned char* smem;
+  int smem_bytes;
 };
 
 struct SharedStep {
@@ -56,21 +58,51 @@ struct SharedStep {
   JacobiShared jsh;
   double norm[NMAX];
   int perm[NMAX];
-  cx<double> v[2][VMAX];
+  zc v[2][VMAX];
   int inst;
 };
 
-template <typename T>
-__device__ __forceinline__ cx<T> to_t(cx<double> a) {
-  return mk<T>((T)a.x, (T)a.y);
-}
-template <typename T>
-__device__ __forceinline__ cx<double> to_d(cx<T> a) {
-  return mk<double>((double)a.x, (double)a.y);
+// Truncated split of the R x N (R >= N) matrix A = op(src): op is the
+// identity (A(row,c) = src[c*lds+row]) or the conjugate transpose
+// (A(row,c) = conj(src[row*lds+c])).  On return *Wout holds A V (FP64,
+// orthogonal columns, ld R), sh.norm / sh.perm / return value as in
+// jacobi_finish.  Shared memory is used for the working matrices that fit.
+template <bool MIXED>
+__device__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel,
+                     Bufs& b, SharedStep& sh, zc** Wout) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  size_t used = 0;
+  auto take = [&](size_t bytes) -> void* {
+    bytes = (bytes + 15) & ~(size_t)15;
+    if (used + bytes > (size_t)b.smem_bytes) return nullptr;
+    void* p = b.smem + used;
+    used += bytes;
+    return p;
+  };
+  cff* Wff = nullptr;
+  if (MIXED) {
+    Wff = (cff*)take((size_t)R * N * sizeof(cff));
+    if (!Wff) Wff = b.Wffg;
+  }
+  zc* W = (zc*)take((size_t)R * N * sizeof(zc));
+  if (!W) W = b.Wg;
+  for (int idx = tid; idx < R * N; idx += nt) {
+    const int c = idx / R, row = idx - c * R;
+    W[idx] = src_trans ? cconj(src[(size_t)row * lds + c]) : src[(size_t)c * lds + row];
+  }
+  __syncthreads();
+  int kk;
+  if (MIXED) {
+    kk = jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh);
+  } else {
+    kk = jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
+  }
+  *Wout = W;
+  return kk;
 }
 
-template <typename T, bool RESCALE>
-__device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T>& b,
+template <bool MIXED>
+__device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& b,
                            SharedStep& sh) {
   const int tid = threadIdx.x;
   const int nt = blockDim.x;
@@ -82,10 +114,12 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
   const long long slot_elems = (long long)cap * D * cap;
   const int step = sh.st.step + 1;
   const long long window = min((long long)step, (long long)I.dkmax + 1);
-  cx<T>* const sites = b.sites + I.site_base;
+  zc* const sites = b.sites + I.site_base;
   int2* const dims = b.dims + I.dims_base;
-  const cx<double>* P1 = b.props + I.prop_base;
-  const cx<double>* P2 = P1 + D * D;
+  const zc* P1 = b.props + I.prop_base;
+  const zc* P2 = P1 + D * D;
+  int splits = 0, sw64 = 0, sw32 = 0;
+  double flops = 0.0;  // algorithmic flops of this step (thread 0's copy is used)
 
 #define SLOT(k) ((sh.st.head + (k)) % I.nslots)
 #define SITE(k) (sites + (long long)SLOT(k) * slot_elems)
@@ -94,13 +128,13 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
   // 1. first half-step propagator on the newest site: A[l][b][0] = sum_a P1[b][a] A[l][a][0]
   {
     const int k = sh.st.nsites - 1;
-    cx<T>* A = SITE(k);
+    zc* A = SITE(k);
     const int l = DIMS(k).x;
     for (int idx = tid; idx < l * D; idx += nt) {
       const int ll = idx / D, bb = idx - ll * D;
-      cx<double> acc = mk<double>(0, 0);
-      for (int a = 0; a < D; ++a) cfma(acc, P1[bb * D + a], to_d(A[ll * D + a]));
-      b.Tg[idx] = to_t<T>(acc);
+      zc acc = mk<double>(0, 0);
+      for (int a = 0; a < D; ++a) cfma(acc, P1[bb * D + a], A[ll * D + a]);
+      b.Tg[idx] = acc;
     }
     __syncthreads();
     for (int idx = tid; idx < l * D; idx += nt) A[idx] = b.Tg[idx];
@@ -109,21 +143,21 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
 
   // 2. trace out the oldest site (sum_north = ones) and merge into the next
   if (sh.st.nsites > window) {
-    cx<T>* A0 = SITE(0);
-    cx<T>* A1 = SITE(1);
+    zc* A0 = SITE(0);
+    zc* A1 = SITE(1);
     const int r0 = DIMS(0).y;
     const int r1 = DIMS(1).y;
     for (int c = tid; c < r0; c += nt) {
-      cx<double> acc = mk<double>(0, 0);
-      for (int a = 0; a < D; ++a) acc = acc + to_d(A0[a * r0 + c]);
+      zc acc = mk<double>(0, 0);
+      for (int a = 0; a < D; ++a) acc = acc + A0[a * r0 + c];
       sh.v[0][c] = acc;
     }
     __syncthreads();
     for (int idx = tid; idx < D * r1; idx += nt) {
       const int a = idx / r1, rr = idx - a * r1;
-      cx<double> acc = mk<double>(0, 0);
-      for (int c = 0; c < r0; ++c) cfma(acc, sh.v[0][c], to_d(A1[((long long)c * D + a) * r1 + rr]));
-      b.Tg[idx] = to_t<T>(acc);
+      zc acc = mk<double>(0, 0);
+      for (int c = 0; c < r0; ++c) cfma(acc, sh.v[0][c], A1[((long long)c * D + a) * r1 + rr]);
+      b.Tg[idx] = acc;
     }
     __syncthreads();
     for (int idx = tid; idx < D * r1; idx += nt) A1[idx] = b.Tg[idx];
@@ -137,194 +171,174 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
   }
 
   const int K = sh.st.nsites;
-  // 3. zip-up
+  // 3. zip-up: theta[(x,a),(r,m)] = I_dk[a,m] sum_c C[x,c,m] A[c,a,r]
   int cxd = 1, ccd = 1;
   for (int k = 0; k < K; ++k) {
-    cx<T>* A = SITE(k);
-    const int2 dA = DIMS(k);
-    const int r = dA.y;
+    zc* A = SITE(k);
+    const int r = DIMS(k).y;
     const int dk = K - 1 - k;
-    const cx<double>* Im = (k == 0 && sh.st.ovr_active) ? (b.props + I.ovr_base)
-                                                         : (b.infl + I.infl_base + (long long)dk * D * D);
+    const zc* Im = (k == 0 && sh.st.ovr_active) ? (b.props + I.ovr_base)
+                                                 : (b.infl + I.infl_base + (long long)dk * D * D);
     const int m = cxd * D;
     const int n = r * D;
-    const cx<T>* C = b.Cg;
-    if (k == K - 1) {
-      for (int idx = tid; idx < m * n; idx += nt) {
-        const int row = idx / n, col = idx - row * n;
-        const int x = row / D, a = row - x * D;
-        const int rr = col / D, mr = col - rr * D;
-        cx<T> acc = mk<T>(0, 0);
-        if (k == 0) {
-          acc = A[a * r + rr];
-        } else {
-          for (int c = 0; c < ccd; ++c)
-            cfma(acc, C[(long long)x * (ccd * D) + c * D + mr], A[((long long)c * D + a) * r + rr]);
-        }
-        b.Tg[idx] = cmul(to_t<T>(Im[a * D + mr]), acc);
-      }
-      __syncthreads();
-      for (int idx = tid; idx < m * n; idx += nt) A[idx] = b.Tg[idx];
-      if (tid == 0) dims[SLOT(k)] = make_int2(cxd, n);
-      __syncthreads();
-      break;
-    }
-    const bool trans = n > m;
-    cx<T>* W = ((long long)m * n <= b.smem_elems) ? b.Ws : b.Wg;
+    const zc* C = b.Cg;
+    const bool last = (k == K - 1);
+    // theta into Tg: column-major (ld m) for a split, site layout for the last site
     for (int idx = tid; idx < m * n; idx += nt) {
-      const int col = idx / m, row = idx - col * m;
+      int row, col;
+      if (last) {
+        row = idx / n;
+        col = idx - row * n;
+      } else {
+        col = idx / m;
+        row = idx - col * m;
+      }
       const int x = row / D, a = row - x * D;
       const int rr = col / D, mr = col - rr * D;
-      cx<T> acc = mk<T>(0, 0);
+      zc acc = mk<double>(0, 0);
       if (k == 0) {
         acc = A[a * r + rr];
       } else {
         for (int c = 0; c < ccd; ++c)
           cfma(acc, C[(long long)x * (ccd * D) + c * D + mr], A[((long long)c * D + a) * r + rr]);
       }
-      const cx<T> th = cmul(to_t<T>(Im[a * D + mr]), acc);
-      b.Tg[idx] = th;
-      if (!trans)
-        W[idx] = th;
-      else
-        W[col + (long long)row * n] = cconj(th);
+      b.Tg[idx] = cmul(Im[a * D + mr], acc);
     }
     __syncthreads();
-    const int kk = trans ? jacobi_truncate<T>(W, n, m, n, I.epsrel, sh.norm, sh.perm, &sh.jsh)
-                         : jacobi_truncate<T>(W, m, n, m, I.epsrel, sh.norm, sh.perm, &sh.jsh);
+    if (last) {
+      for (int idx = tid; idx < m * n; idx += nt) A[idx] = b.Tg[idx];
+      if (tid == 0) dims[SLOT(k)] = make_int2(cxd, n);
+      __syncthreads();
+      break;
+    }
+    const bool trans = n > m;
+    zc* W;
+    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, b, sh, &W)
+                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, b, sh, &W);
+    {
+      const double R = trans ? n : m, N = trans ? m : n;
+      flops += 8.0 * m * n * ccd + 4.0 * (6.0 * R * N * N + 20.0 * N * N * N);
+    }
+    ++splits;
+    sw64 += sh.jsh.sweeps;
+    sw32 += sh.jsh.sweeps32;
     if (sh.jsh.status != ST_OK || kk > cap) {
       if (tid == 0) sh.st.status = (sh.jsh.status != ST_OK) ? sh.jsh.status : ST_CHI_OVERFLOW;
       __syncthreads();
       break;
     }
-    const double smax = sh.norm[sh.perm[0]];
-    const T cscal = RESCALE ? (T)(1.0 / smax) : (T)1;
-    cx<T>* Cn = b.Cg;  // new carry overwrites the old one (old one no longer read)
     if (!trans) {
       // U = W[:, perm] / s  -> site (cxd, D, kk);  carry = U^H theta
       for (int idx = tid; idx < m * kk; idx += nt) {
         const int row = idx / kk, j = idx - row * kk;
         const int pj = sh.perm[j];
-        const T inv = (T)(1.0 / sh.norm[pj]);
-        A[idx] = cscale(W[(long long)pj * m + row], inv);
+        A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
       }
       for (int idx = tid; idx < kk * n; idx += nt) {
         const int j = idx / n, col = idx - j * n;
         const int pj = sh.perm[j];
-        const cx<T>* u = W + (long long)pj * m;
-        const cx<T>* th = b.Tg + (long long)col * m;
-        cx<T> acc = mk<T>(0, 0);
+        const zc* u = W + (long long)pj * m;
+        const zc* th = b.Tg + (long long)col * m;
+        zc acc = mk<double>(0, 0);
         for (int row = 0; row < m; ++row) cjfma(acc, u[row], th[row]);
-        Cn[idx] = cscale(acc, (T)(1.0 / sh.norm[pj]) * cscal);
+        b.Cg[idx] = cscale(acc, 1.0 / sh.norm[pj]);
       }
     } else {
-      // W = theta^H orthogonalised: U = theta W[:, perm] / s^2, carry = W[:, perm]^H
+      // W = theta^H V orthogonal: U = theta W[:, perm] / s^2, carry = W[:, perm]^H
       for (int idx = tid; idx < m * kk; idx += nt) {
         const int row = idx / kk, j = idx - row * kk;
         const int pj = sh.perm[j];
         const double sj = sh.norm[pj];
-        const cx<T>* w = W + (long long)pj * n;
-        cx<T> acc = mk<T>(0, 0);
+        const zc* w = W + (long long)pj * n;
+        zc acc = mk<double>(0, 0);
         for (int col = 0; col < n; ++col) cfma(acc, b.Tg[(long long)col * m + row], w[col]);
-        A[idx] = cscale(acc, (T)(1.0 / (sj * sj)));
+        A[idx] = cscale(acc, 1.0 / (sj * sj));
       }
       for (int idx = tid; idx < kk * n; idx += nt) {
         const int j = idx / n, col = idx - j * n;
-        Cn[idx] = cscale(cconj(W[(long long)sh.perm[j] * n + col]), cscal);
+        b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
       }
     }
-    if (tid == 0) {
-      dims[SLOT(k)] = make_int2(cxd, kk);
-      if (RESCALE) sh.st.log_scale += log(smax);
-    }
+    if (tid == 0) dims[SLOT(k)] = make_int2(cxd, kk);
     __syncthreads();
     cxd = kk;
     ccd = r;
   }
-  if (sh.st.status != ST_OK) {
-    if (tid == 0) L.state[i] = sh.st;
-    return;
-  }
 
-  // 4. right-to-left sweep
-  for (int k = K - 1; k >= 1; --k) {
-    cx<T>* A = SITE(k);
-    const int2 dA = DIMS(k);
-    const int l = dA.x, r = dA.y;
-    const int m = D * r, n = l;
-    const bool trans = n > m;
-    cx<T>* W = ((long long)m * n <= b.smem_elems) ? b.Ws : b.Wg;
-    if (!trans) {
-      for (int idx = tid; idx < m * n; idx += nt) W[idx] = A[idx];
-    } else {
-      for (int idx = tid; idx < m * n; idx += nt) {
-        const int col = idx / m, row = idx - col * m;
-        W[col + (long long)row * n] = cconj(A[idx]);
+  // 4. right-to-left sweep: site k as the column-major (D r) x l matrix
+  if (sh.st.status == ST_OK) {
+    for (int k = K - 1; k >= 1; --k) {
+      zc* A = SITE(k);
+      const int2 dA = DIMS(k);
+      const int l = dA.x, r = dA.y;
+      const int m = D * r, n = l;
+      const bool trans = n > m;
+      zc* W;
+      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, b, sh, &W)
+                           : split<MIXED>(A, m, false, m, n, I.epsrel, b, sh, &W);
+      {
+        const double R = trans ? n : m, N = trans ? m : n;
+        flops += 4.0 * (6.0 * R * N * N + 20.0 * N * N * N) + 8.0 * DIMS(k - 1).x * D * (double)kk * n;
       }
-    }
-    __syncthreads();
-    const int kk = trans ? jacobi_truncate<T>(W, n, m, n, I.epsrel, sh.norm, sh.perm, &sh.jsh)
-                         : jacobi_truncate<T>(W, m, n, m, I.epsrel, sh.norm, sh.perm, &sh.jsh);
-    if (sh.jsh.status != ST_OK || kk > cap) {
-      if (tid == 0) sh.st.status = (sh.jsh.status != ST_OK) ? sh.jsh.status : ST_CHI_OVERFLOW;
+      ++splits;
+      sw64 += sh.jsh.sweeps;
+      sw32 += sh.jsh.sweeps32;
+      if (sh.jsh.status != ST_OK || kk > cap) {
+        if (tid == 0) sh.st.status = (sh.jsh.status != ST_OK) ? sh.jsh.status : ST_CHI_OVERFLOW;
+        __syncthreads();
+        break;
+      }
+      if (!trans) {
+        for (int idx = tid; idx < kk * n; idx += nt) {
+          const int j = idx / n, col = idx - j * n;
+          const int pj = sh.perm[j];
+          const zc* u = W + (long long)pj * m;
+          const zc* y = A + (long long)col * m;
+          zc acc = mk<double>(0, 0);
+          for (int row = 0; row < m; ++row) cjfma(acc, u[row], y[row]);
+          b.Cg[idx] = cscale(acc, 1.0 / sh.norm[pj]);
+        }
+        __syncthreads();
+        for (int idx = tid; idx < m * kk; idx += nt) {
+          const int j = idx / m, row = idx - j * m;
+          const int pj = sh.perm[j];
+          A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
+        }
+      } else {
+        for (int idx = tid; idx < m * kk; idx += nt) {
+          const int j = idx / m, row = idx - j * m;
+          const int pj = sh.perm[j];
+          const double sj = sh.norm[pj];
+          const zc* w = W + (long long)pj * n;
+          zc acc = mk<double>(0, 0);
+          for (int col = 0; col < n; ++col) cfma(acc, A[(long long)col * m + row], w[col]);
+          b.Tg[idx] = cscale(acc, 1.0 / (sj * sj));
+        }
+        for (int idx = tid; idx < kk * n; idx += nt) {
+          const int j = idx / n, col = idx - j * n;
+          b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
+        }
+        __syncthreads();
+        for (int idx = tid; idx < m * kk; idx += nt) A[idx] = b.Tg[idx];
+      }
+      if (tid == 0) dims[SLOT(k)] = make_int2(kk, r);
       __syncthreads();
-      break;
-    }
-    const double smax = sh.norm[sh.perm[0]];
-    const T cscal = RESCALE ? (T)(1.0 / smax) : (T)1;
-    if (!trans) {
-      for (int idx = tid; idx < kk * n; idx += nt) {
-        const int j = idx / n, col = idx - j * n;
-        const int pj = sh.perm[j];
-        const cx<T>* u = W + (long long)pj * m;
-        const cx<T>* y = A + (long long)col * m;
-        cx<T> acc = mk<T>(0, 0);
-        for (int row = 0; row < m; ++row) cjfma(acc, u[row], y[row]);
-        b.Cg[idx] = cscale(acc, (T)(1.0 / sh.norm[pj]) * cscal);
+      // absorb S V^H into site k-1: (l2, D, n) x (kk, n)^T -> (l2, D, kk)
+      zc* B = SITE(k - 1);
+      const int l2 = DIMS(k - 1).x;
+      for (int idx = tid; idx < l2 * D * kk; idx += nt) {
+        const int la = idx / kk, j = idx - la * kk;
+        const zc* brow = B + (long long)la * n;
+        const zc* crow = b.Cg + (long long)j * n;
+        zc acc = mk<double>(0, 0);
+        for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
+        b.Tg[idx] = acc;
       }
       __syncthreads();
-      for (int idx = tid; idx < m * kk; idx += nt) {
-        const int j = idx / m, row = idx - j * m;
-        const int pj = sh.perm[j];
-        A[idx] = cscale(W[(long long)pj * m + row], (T)(1.0 / sh.norm[pj]));
-      }
-    } else {
-      for (int idx = tid; idx < m * kk; idx += nt) {
-        const int j = idx / m, row = idx - j * m;
-        const int pj = sh.perm[j];
-        const double sj = sh.norm[pj];
-        const cx<T>* w = W + (long long)pj * n;
-        cx<T> acc = mk<T>(0, 0);
-        for (int col = 0; col < n; ++col) cfma(acc, A[(long long)col * m + row], w[col]);
-        b.Tg[idx] = cscale(acc, (T)(1.0 / (sj * sj)));
-      }
-      for (int idx = tid; idx < kk * n; idx += nt) {
-        const int j = idx / n, col = idx - j * n;
-        b.Cg[idx] = cscale(cconj(W[(long long)sh.perm[j] * n + col]), cscal);
-      }
+      for (int idx = tid; idx < l2 * D * kk; idx += nt) B[idx] = b.Tg[idx];
+      if (tid == 0) dims[SLOT(k - 1)] = make_int2(l2, kk);
       __syncthreads();
-      for (int idx = tid; idx < m * kk; idx += nt) A[idx] = b.Tg[idx];
     }
-    if (tid == 0) {
-      dims[SLOT(k)] = make_int2(kk, r);
-      if (RESCALE) sh.st.log_scale += log(smax);
-    }
-    __syncthreads();
-    // absorb S V^H into site k-1: (l2, D, n) x (kk, n)^T -> (l2, D, kk)
-    cx<T>* B = SITE(k - 1);
-    const int l2 = DIMS(k - 1).x;
-    for (int idx = tid; idx < l2 * D * kk; idx += nt) {
-      const int la = idx / kk, j = idx - la * kk;
-      const cx<T>* brow = B + (long long)la * n;
-      const cx<T>* crow = b.Cg + (long long)j * n;
-      cx<T> acc = mk<T>(0, 0);
-      for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
-      b.Tg[idx] = acc;
-    }
-    __syncthreads();
-    for (int idx = tid; idx < l2 * D * kk; idx += nt) B[idx] = b.Tg[idx];
-    if (tid == 0) dims[SLOT(k - 1)] = make_int2(l2, kk);
-    __syncthreads();
   }
   if (sh.st.status != ST_OK) {
     if (tid == 0) L.state[i] = sh.st;
@@ -333,10 +347,10 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
 
   // 5. second half-step propagator as the new last site: A[r][b][0] = P2[b][r]
   {
-    cx<T>* A = SITE(K);
+    zc* A = SITE(K);
     for (int idx = tid; idx < D * D; idx += nt) {
       const int rr = idx / D, bb = idx - rr * D;
-      A[idx] = to_t<T>(P2[bb * D + rr]);
+      A[idx] = P2[bb * D + rr];
     }
     if (tid == 0) {
       dims[SLOT(K)] = make_int2(D, 1);
@@ -352,15 +366,15 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
     __syncthreads();
     int maxb = 1;
     for (int k = 0; k < K; ++k) {
-      const cx<T>* A = SITE(k);
+      const zc* A = SITE(k);
       const int2 dA = DIMS(k);
       const int l = dA.x, r = dA.y;
       maxb = max(maxb, r);
       for (int rr = tid; rr < r; rr += nt) {
-        cx<double> acc = mk<double>(0, 0);
+        zc acc = mk<double>(0, 0);
         for (int c = 0; c < l; ++c) {
-          cx<double> part = mk<double>(0, 0);
-          for (int a = 0; a < D; ++a) part = part + to_d(A[((long long)c * D + a) * r + rr]);
+          zc part = mk<double>(0, 0);
+          for (int a = 0; a < D; ++a) part = part + A[((long long)c * D + a) * r + rr];
           cfma(acc, sh.v[cur][c], part);
         }
         sh.v[cur ^ 1][rr] = acc;
@@ -369,19 +383,18 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
       cur ^= 1;
     }
     if (tid < D) {
-      cx<double> acc = mk<double>(0, 0);
+      zc acc = mk<double>(0, 0);
       for (int c = 0; c < D; ++c) cfma(acc, P2[tid * D + c], sh.v[cur][c]);
-      if (RESCALE) {
-        const double f = exp(sh.st.log_scale);
-        acc.x *= f;
-        acc.y *= f;
-      }
       b.out[I.out_base + (long long)(step % I.out_cap) * D + tid] = acc;
     }
     if (tid == 0) {
       sh.st.step = step;
       sh.st.max_bond = maxb;
       sh.st.ovr_active = 0;
+      sh.st.splits += splits;
+      sh.st.sweeps64 += sw64;
+      sh.st.sweeps32 += sw32;
+      sh.st.flops_alg += flops;
       L.state[i] = sh.st;
     }
     __syncthreads();
@@ -391,22 +404,23 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs<T
 #undef DIMS
 }
 
-template <typename T, bool RESCALE>
+template <bool MIXED>
 __global__ void __launch_bounds__(TEMPO_THREADS) tempo_kernel(TempoLaunch L) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ SharedStep sh;
-  Bufs<T> b;
-  b.sites = (cx<T>*)L.sites;
+  Bufs b;
+  b.sites = (zc*)L.sites;
   b.dims = L.dims;
-  b.infl = (const cx<double>*)L.infl;
-  b.props = (const cx<double>*)L.props;
-  b.out = (cx<double>*)L.out;
-  cx<T>* work = (cx<T>*)L.work + (long long)blockIdx.x * L.work_stride;
-  b.Wg = work;
-  b.Tg = work + L.wcap;
-  b.Cg = work + 2 * L.wcap;
-  b.Ws = (cx<T>*)dsm;
-  b.smem_elems = L.smem_elems;
+  b.infl = (const zc*)L.infl;
+  b.props = (const zc*)L.props;
+  b.out = (zc*)L.out;
+  unsigned char* work = (unsigned char*)L.work + (long long)blockIdx.x * L.work_stride;
+  b.Wg = (zc*)work;
+  b.Tg = b.Wg + L.wcap;
+  b.Cg = b.Tg + L.wcap;
+  b.Wffg = (cff*)(b.Cg + L.wcap);
+  b.smem = dsm;
+  b.smem_bytes = L.smem_bytes;
   for (;;) {
     if (threadIdx.x == 0) sh.inst = atomicAdd(L.queue, 1);
     __syncthreads();
@@ -416,7 +430,7 @@ __global__ void __launch_bounds__(TEMPO_THREADS) tempo_kernel(TempoLaunch L) {
     const int i = L.order[q];
     const InstDev I = L.inst[i];
     for (int s = 0; s < L.nsteps; ++s) {
-      tempo_step<T, RESCALE>(L, I, i, b, sh);
+      tempo_step<MIXED>(L, I, i, b, sh);
       __syncthreads();
       if (sh.st.status != ST_OK) break;
     }
@@ -424,28 +438,27 @@ __global__ void __launch_bounds__(TEMPO_THREADS) tempo_kernel(TempoLaunch L) {
 }
 
 int tempo_smem_bytes(int precision) {
-  // 80 KiB of dynamic shared memory for the working matrix: two CTAs per SM
-  // together with the static SharedStep block.
+  // dynamic shared memory for the working matrices: two CTAs per SM
+  // together with the static SharedStep block
   (void)precision;
-  return 80 * 1024;
+  return 88 * 1024;
 }
 
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
                          cudaStream_t stream) {
   const int smem = tempo_smem_bytes(precision);
   TempoLaunch l2 = L;
+  l2.smem_bytes = smem;
   if (precision == 0) {
-    l2.smem_elems = smem / (int)sizeof(cx<double>);
-    cudaError_t e = cudaFuncSetAttribute(tempo_kernel<double, false>,
+    cudaError_t e = cudaFuncSetAttribute(tempo_kernel<false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    tempo_kernel<double, false><<<grid, block, smem, stream>>>(l2);
+    tempo_kernel<false><<<grid, block, smem, stream>>>(l2);
   } else {
-    l2.smem_elems = smem / (int)sizeof(cx<float>);
-    cudaError_t e = cudaFuncSetAttribute(tempo_kernel<float, true>,
+    cudaError_t e = cudaFuncSetAttribute(tempo_kernel<true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    tempo_kernel<float, true><<<grid, block, smem, stream>>>(l2);
+    tempo_kernel<true><<<grid, block, smem, stream>>>(l2);
   }
   return cudaGetLastError();
 }

@@ -123,7 +123,9 @@ class TempoBatch:
         inf = nat.TempoInfo()
         nat.check(nat.lib().otb_tempo_get_info(self._h, int(i), ctypes.byref(inf)))
         return {"step": inf.step, "status": inf.status, "nsites": inf.nsites,
-                "max_bond": inf.max_bond, "log_scale": inf.log_scale}
+                "max_bond": inf.max_bond, "log_scale": inf.log_scale,
+                "splits": inf.splits, "sweeps64": inf.sweeps64,
+                "sweeps32": inf.sweeps32, "flops_alg": inf.flops_alg}
 
     def check_status(self):
         for i in range(self.n):

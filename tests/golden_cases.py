@@ -65,7 +65,10 @@ PARITY_ABS = 1e-10     # trace distance on rounding-insensitive steps
 ENVELOPE_FACTOR = 10.0  # allowance over the reference's own rounding spread
 
 
-def parity_violations(errors, envelope):
+MIXED_ABS = 1e-6       # the mixed-precision form's trace-distance bar
+
+
+def parity_violations(errors, envelope, abs_tol=PARITY_ABS):
     """Steps where ``errors`` (per-step trace distance to the reference)
     exceeds ``max(PARITY_ABS, ENVELOPE_FACTOR * envelope)``.
 
@@ -79,10 +82,10 @@ def parity_violations(errors, envelope):
     # A rounding-level tie persists once it has happened, and two perturbed
     # runs sample its amplitude only roughly, so every step from the first
     # sensitive one on is held to the run's largest spread.
-    tol = np.full(env.shape, PARITY_ABS)
+    tol = np.full(env.shape, abs_tol)
     sensitive = env > PARITY_ABS
     if sensitive.any():
         first = int(np.argmax(sensitive))
-        tol[first:] = max(PARITY_ABS, ENVELOPE_FACTOR * float(env.max()))
+        tol[first:] = max(abs_tol, ENVELOPE_FACTOR * float(env.max()))
     return [(i, float(e), float(t)) for i, (e, t) in
             enumerate(zip(errors, tol)) if e > t]

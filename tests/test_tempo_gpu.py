@@ -77,10 +77,15 @@ def test_gpu_tempo_batch_mixed_memory_lengths():
 
 
 @pytest.mark.parametrize("name", ["config1_spin_boson", "nondiag_coupling",
-                                  "batched_like_hot"])
-def test_gpu_tempo_mixed_precision_error(name):
+                                  "add_corr_time", "batched_like_hot"])
+def test_gpu_tempo_mixed_precision_matches_reference(name):
+    """The mixed form (double-float Jacobi on the FP32 pipe, FP64 rank
+    decisions): trace distance <= 1e-6 against the reference, or within
+    ENVELOPE_FACTOR x the reference's own rounding envelope once that
+    exceeds 1e-10."""
     g = gc.load(name)
     states, _ = _run_backend(g, "mixed")
-    err = to.max_trace_distance(states, g["tempo_states"])
-    print(f"{name}: mixed-precision max trace distance {err:.2e}")
-    assert err < 1e-4
+    errs = [to.trace_distance(a, b) for a, b in zip(states, g["tempo_states"])]
+    print(f"{name}: mixed-precision max trace distance {max(errs):.2e}")
+    bad = gc.parity_violations(errs, g["tempo_envelope"], gc.MIXED_ABS)
+    assert not bad, bad[:5]
