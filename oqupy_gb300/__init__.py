@@ -8,5 +8,7 @@ select through ``backend_config={"backend": "gb300", ...}`` once
 """
 
 from .tempo import TempoBatch, GpuTempoBackend, fold_propagators  # noqa: F401
+from .install import install, uninstall  # noqa: F401
 
-__all__ = ["TempoBatch", "GpuTempoBackend", "fold_propagators"]
+__all__ = ["TempoBatch", "GpuTempoBackend", "fold_propagators", "install",
+           "uninstall"]

@@ -53,6 +53,14 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
 // acc + a * b
 __device__ __forceinline__ ff ff_fma(ff a, ff b, ff acc) { return ff_add(acc, ff_mul(a, b)); }
 
+// 1/sqrt(u) for u > 0: float estimate refined by one Newton step in FF
+__device__ __forceinline__ ff ff_rsqrt(ff u) {
+  const float y0 = rsqrtf(u.hi);
+  const ff y = ff_make(y0, 0.f);
+  const ff e = ff_sub(ff_make(1.f, 0.f), ff_mul(u, ff_mul(y, y)));
+  return ff_add(y, ff_mul(ff_make(0.5f * y0, 0.f), e));
+}
+
 __device__ __forceinline__ ff ff_shfl_xor(ff v, int off) {
   return ff_make(__shfl_xor_sync(0xffffffffu, v.hi, off, 32), __shfl_xor_sync(0xffffffffu, v.lo, off, 32));
 }

@@ -188,8 +188,8 @@ __device__ int jacobi_sweeps(cx<T>* W, int m, int n, int ld, cx<T>* V, int ldv, 
 
 // One-sided Jacobi sweeps in double-float arithmetic on W (m x n, ld).
 // Same schedule, stopping test and numerical-zero floor as jacobi_sweeps;
-// the inner products are reduced in FF, the rotation angle is computed in
-// FP64 from them, and the rotation is applied in FF.  Orthogonality reaches
+// the inner products are reduced in FF, the rotation parameters are formed
+// on the FP32 pipe (see below), and the rotation is applied in FF.  Orthogonality reaches
 // about 1e-14 relative, with every per-element operation on the FP32 pipe.
 __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShared* sh) {
   const int tid = threadIdx.x;
@@ -200,29 +200,26 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
   const int ngroups = nthreads / G;
   const int np = (n + 1) >> 1;
   const int nn = np << 1;
-  const double eps_ff = 3.6e-15;  // ~2^-48, double-float unit roundoff
-  const double tol = sqrt((double)m) * eps_ff;
+  const float eps_ff = 3.6e-15f;  // ~2^-48, double-float unit roundoff
+  const float tol = sqrtf((float)m) * eps_ff;
   if (tid == 0) sh->flag[0] = 0;
   __syncthreads();
   if (n <= 1) return 0;
   int sweep;
   for (sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
-    double zfloor;
+    float zfloor;
     {
-      double mx = 0.0;
+      float mx = 0.f;
       for (int j = tid / 32; j < n; j += nthreads / 32) {
         const int l = tid & 31;
-        double acc = 0.0;
+        float acc = 0.f;
         const cff* c = W + (size_t)j * ld;
-        for (int r = l; r < m; r += 32) {
-          const double x = (double)c[r].x.hi, y = (double)c[r].y.hi;
-          acc = fma(x, x, fma(y, y, acc));
-        }
+        for (int r = l; r < m; r += 32) acc = fmaf(c[r].x.hi, c[r].x.hi, fmaf(c[r].y.hi, c[r].y.hi, acc));
         for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        mx = fmax(mx, acc);
+        mx = fmaxf(mx, acc);
       }
-      for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-      if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
+      for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      if ((tid & 31) == 0) sh->red[tid >> 5] = (double)mx;
       __syncthreads();
       if (tid == 0) {
         double v = 0.0;
@@ -230,8 +227,8 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
         sh->red[32] = v;
       }
       __syncthreads();
-      const double zf = 16.0 * sqrt((double)m) * eps_ff;
-      zfloor = zf * zf * sh->red[32];
+      const float zf = 16.f * sqrtf((float)m) * eps_ff;
+      zfloor = zf * zf * (float)sh->red[32];
     }
     for (int round = 0; round < nn - 1; ++round) {
       for (int pb = 0; pb < np; pb += ngroups) {
@@ -270,20 +267,28 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
           gi = ff_add(gi, ff_shfl_xor(gi, off));
         }
         if (active) {
-          const double A = ff_to(al), B = ff_to(be), Gr = ff_to(gr), Gi = ff_to(gi);
-          const double g = sqrt(Gr * Gr + Gi * Gi);
-          if (A > zfloor && B > zfloor && g > tol * sqrt(A) * sqrt(B)) {
-            const double zeta = (B - A) / (2 * g);
-            const double az = fabs(zeta);
-            double t = (az > 1e150) ? 0.5 / az : 1.0 / (az + sqrt(1.0 + zeta * zeta));
-            if (zeta < 0) t = -t;
-            const double c = 1.0 / sqrt(1.0 + t * t);
-            const double s = c * t;
-            const double pr = Gr / g, pi = Gi / g;
-            const ff fc = ff_from(c);
+          // Rotation parameters on the FP32 pipe.  The angle only needs float
+          // accuracy (later sweeps correct it); unitarity is what must hold to
+          // FF precision, so c, s come from t through an FF rsqrt
+          // (c^2 + s^2 = c^2 (1 + t^2) = 1) and the phase is normalised in FF.
+          const float A = al.hi, B = be.hi;
+          const float g = hypotf(gr.hi, gi.hi);
+          if (A > zfloor && B > zfloor && g > tol * sqrtf(A) * sqrtf(B)) {
+            const float zeta = (B - A) / (2.f * g);
+            const float az = fabsf(zeta);
+            float t = (az > 1e18f) ? 0.5f / az : 1.f / (az + sqrtf(1.f + zeta * zeta));
+            if (zeta < 0.f) t = -t;
+            const ff ft = ff_make(t, 0.f);
+            const ff fc = ff_rsqrt(ff_add(ff_make(1.f, 0.f), ff_mul(ft, ft)));
+            const ff fs = ff_mul(fc, ft);
+            const ff ig = ff_make(1.f / g, 0.f);
+            const ff px = ff_mul(gr, ig), py = ff_mul(gi, ig);
+            const ff nrm = ff_rsqrt(ff_add(ff_mul(px, px), ff_mul(py, py)));
+            const ff pr = ff_mul(px, nrm), pi = ff_mul(py, nrm);
             // q = s e^{-i phi}, w = s e^{i phi}
-            const ff qx = ff_from(s * pr), qy = ff_from(-s * pi);
-            const ff wy = ff_from(s * pi);
+            const ff qx = ff_mul(fs, pr);
+            const ff wy = ff_mul(fs, pi);
+            const ff qy = ff_make(-wy.hi, -wy.lo);
             for (int r = lane; r < m; r += G) {
               const cff u = ca[r];
               const cff v = cb[r];
