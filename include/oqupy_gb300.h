@@ -119,6 +119,73 @@ otb_status otb_tempo_set_first_influence(otb_tempo* h, int32_t inst,
 /* Grow the site ring of every instance to at least nslots slots. */
 otb_status otb_tempo_reserve_sites(otb_tempo* h, int32_t nslots);
 
+/* --------------------------------------------------------------- PT-TEMPO */
+
+typedef struct otb_pt otb_pt;
+
+typedef struct {
+  int32_t precision;   /* OTB_PRECISION_* */
+  int32_t chi_cap;     /* bond-dimension capacity of every site, chi_cap * D <= 1152 */
+  int32_t grid;        /* CTAs per launch, 0 = 2 per SM */
+} otb_pt_config;
+
+typedef struct {
+  int32_t hs_dim;             /* d (D = d*d <= 9) */
+  int32_t num_steps;          /* process-tensor length (>= 2) */
+  int32_t dkmax;              /* memory length; num_infl = min(num_steps, dkmax+1) >= 2 */
+  double epsrel;
+  const double* influences;   /* num_infl * D * D complex, dk = 0..num_infl-1,
+                                 coupling eigenbasis, [dk][a][r] */
+  const double* neg_influences; /* (num_steps+1) * D * D indexed by step for the
+                                   grow-phase dk = -step influences, or NULL */
+} otb_pt_instance;
+
+typedef struct {
+  int32_t step;       /* 0 = not initialised; num_steps = done */
+  int32_t status;
+  int32_t num_steps;
+  int32_t max_bond;
+  int32_t splits;
+  int32_t sweeps64;
+  int32_t sweepsff;
+  int32_t caps_done;
+  double flops_alg;
+} otb_pt_info;
+
+/* Replaces PtTempoBackend.__init__ (pt_tempo_backend.py:56-93), batched. */
+otb_status otb_pt_create(const otb_pt_config* cfg, int32_t n_instances,
+                         const otb_pt_instance* instances, otb_pt** out);
+void otb_pt_destroy(otb_pt* h);
+/* Replaces PtTempoBackend.initialize (first call) and nsteps calls of
+ * compute_step (pt_tempo_backend.py:105-282); computes the caps
+ * (process_tensor.py:380-406) once the build is complete. */
+otb_status otb_pt_advance(otb_pt* h, int32_t nsteps, void* stream);
+otb_status otb_pt_get_info(otb_pt* h, int32_t inst, otb_pt_info* info);
+/* num_steps+1 bond dimensions (process_tensor.py:367-378). */
+otb_status otb_pt_bond_dims(otb_pt* h, int32_t inst, int32_t* out, int32_t cap);
+/* Rank-3 PT-MPO tensor of one step, [past bond][future bond][D] complex,
+ * already multiplied by d (pt_tempo_backend.py:284-307); dims[0..1] get the
+ * bond dimensions, out must hold cap_elems complex values. */
+otb_status otb_pt_get_tensor(otb_pt* h, int32_t inst, int32_t step, double* out,
+                             int64_t cap_elems, int32_t* dims);
+/* Cap vector of one step (process_tensor.py:358-365); *count gets its length. */
+otb_status otb_pt_get_cap(otb_pt* h, int32_t inst, int32_t step, double* out,
+                          int32_t cap, int32_t* count);
+
+/* ------------------------------------------------------ process-tensor sweep */
+
+/* compute_dynamics over one built process tensor for n_systems systems at
+ * once (system_dynamics.py:41-182 with no controls, record_all=True):
+ * prop1/prop2 are n_systems * D * D complex half-step propagators (with any
+ * transform_in / transform_out of the process tensor folded in: P1 <- Tin^T P1,
+ * P2 <- P2 Tout^T), rho0 is n_systems * D, out receives
+ * (num_steps+1) * n_systems * D complex.  The num_steps launches are replayed
+ * as one CUDA graph. */
+otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t n_systems,
+                       const double* prop1, const double* prop2,
+                       const double* rho0, int32_t num_steps, double* out,
+                       void* stream);
+
 /* Measured FMA-pipe throughput of this GPU (TFLOP/s, 2 flops per FMA):
  * precision 0 = FP64 (DFMA), 1 = FP32 (FFMA).  Used as the roofline peak of
  * the Jacobi kernels, which run on these pipes. */

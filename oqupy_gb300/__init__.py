@@ -8,7 +8,8 @@ select through ``backend_config={"backend": "gb300", ...}`` once
 """
 
 from .tempo import TempoBatch, GpuTempoBackend, fold_propagators  # noqa: F401
+from .pt import PtBatch, GpuPtTempoBackend, device_compute_dynamics  # noqa: F401
 from .install import install, uninstall  # noqa: F401
 
-__all__ = ["TempoBatch", "GpuTempoBackend", "fold_propagators", "install",
-           "uninstall"]
+__all__ = ["TempoBatch", "GpuTempoBackend", "fold_propagators", "PtBatch",
+           "GpuPtTempoBackend", "device_compute_dynamics", "install", "uninstall"]

@@ -59,6 +59,25 @@ class TempoInfo(ctypes.Structure):
                 ("flops_alg", ctypes.c_double)]
 
 
+class PtConfig(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("chi_cap", ctypes.c_int32),
+                ("grid", ctypes.c_int32)]
+
+
+class PtInstance(ctypes.Structure):
+    _fields_ = [("hs_dim", ctypes.c_int32), ("num_steps", ctypes.c_int32),
+                ("dkmax", ctypes.c_int32), ("epsrel", ctypes.c_double),
+                ("influences", c_double_p), ("neg_influences", c_double_p)]
+
+
+class PtInfo(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("num_steps", ctypes.c_int32), ("max_bond", ctypes.c_int32),
+                ("splits", ctypes.c_int32), ("sweeps64", ctypes.c_int32),
+                ("sweepsff", ctypes.c_int32), ("caps_done", ctypes.c_int32),
+                ("flops_alg", ctypes.c_double)]
+
+
 class DeviceError(RuntimeError):
     """A status code returned by the CUDA library."""
 
@@ -86,6 +105,16 @@ def _declare(lib):
         "otb_tempo_set_propagators": (i32, [P, i32, c_double_p, c_double_p]),
         "otb_tempo_set_first_influence": (i32, [P, i32, c_double_p]),
         "otb_tempo_reserve_sites": (i32, [P, i32]),
+        "otb_pt_create": (i32, [ctypes.POINTER(PtConfig), i32,
+                                ctypes.POINTER(PtInstance), ctypes.POINTER(P)]),
+        "otb_pt_destroy": (None, [P]),
+        "otb_pt_advance": (i32, [P, i32, P]),
+        "otb_pt_get_info": (i32, [P, i32, ctypes.POINTER(PtInfo)]),
+        "otb_pt_bond_dims": (i32, [P, i32, c_int32_p, i32]),
+        "otb_pt_get_tensor": (i32, [P, i32, i32, c_double_p, ctypes.c_int64, c_int32_p]),
+        "otb_pt_get_cap": (i32, [P, i32, i32, c_double_p, i32, c_int32_p]),
+        "otb_dyn_run": (i32, [P, i32, i32, c_double_p, c_double_p, c_double_p, i32,
+                              c_double_p, P]),
         "otb_measure_fma_peak": (i32, [i32, c_double_p]),
         "otb_last_error": (ctypes.c_char_p, []),
         "otb_version": (i32, []),
@@ -104,8 +133,10 @@ def exported_symbols():
         "otb_tempo_read_states", "otb_tempo_read_all_states",
         "otb_tempo_get_info", "otb_tempo_bond_dims", "otb_tempo_set_influence",
         "otb_tempo_set_propagators", "otb_tempo_set_first_influence",
-        "otb_tempo_reserve_sites", "otb_measure_fma_peak", "otb_last_error",
-        "otb_version"]
+        "otb_tempo_reserve_sites", "otb_pt_create", "otb_pt_destroy",
+        "otb_pt_advance", "otb_pt_get_info", "otb_pt_bond_dims",
+        "otb_pt_get_tensor", "otb_pt_get_cap", "otb_dyn_run",
+        "otb_measure_fma_peak", "otb_last_error", "otb_version"]
 
 
 def fma_peak_tflops(precision: int) -> float:

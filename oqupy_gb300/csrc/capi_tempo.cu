@@ -169,6 +169,7 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     I.cap = h->cap;
     I.epsrel = s.epsrel;
     I.out_cap = h->out_cap;
+    I.out_origin = 0;
     const int want = full ? std::max(s.max_sites, 8) : s.dkmax + 2;
     nslots[i] = std::max(want, 2);
     const int ninfl = full ? s.n_influences : s.dkmax + 1;

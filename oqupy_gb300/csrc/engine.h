@@ -21,6 +21,7 @@ struct InstDev {
   long long prop_base;   // element offset of P1 (D*D), P2 (D*D), rho0 (D)
   long long out_base;    // element offset of the state output ring (out_cap * D)
   long long ovr_base;    // element offset of the first-site override influence (D*D)
+  int out_origin;        // state of step s goes to ring entry (s - out_origin) % out_cap
 };
 
 // Mutable per-instance state (device array).
@@ -66,5 +67,80 @@ inline long long tempo_work_bytes(long long wcap) { return wcap * (3 * 16 + 16);
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
                          cudaStream_t stream);
 int tempo_smem_bytes(int precision);
+
+// ---------------------------------------------------------------- PT-TEMPO
+
+struct PtDev {
+  int D;              // Liouville dimension
+  int d;              // Hilbert dimension
+  int num_steps;      // MPS length at the end of the build
+  int num_infl;       // min(num_steps, dkmax + 1)
+  int cap;            // bond-dimension capacity per site
+  int has_neg;        // grow-phase influences for dk = -step supplied
+  double epsrel;
+  long long site_base;  // num_steps slots of cap * D * cap
+  long long dims_base;  // num_steps int2
+  long long infl_base;  // num_infl * D * D, dk = 0 .. num_infl-1
+  long long neg_base;   // (num_steps + 1) * D * D, indexed by step
+  long long caps_base;  // (num_steps + 1) * cap
+};
+
+struct PtState {
+  int step;      // 0 = not initialised, then 1 .. num_steps
+  int nsites;
+  int mpo_len;
+  int status;
+  int splits;
+  int sweeps64;
+  int sweepsff;
+  int caps_done;
+  double flops_alg;
+};
+
+struct PtLaunch {
+  int n;
+  const PtDev* inst;
+  PtState* state;
+  int2* dims;
+  void* sites;
+  const double* infl;
+  const double* neg;
+  double* caps;
+  void* work;
+  long long work_stride;  // bytes per CTA
+  long long wcap;         // complex elements of one matrix buffer
+  int* queue;
+  const int* order;
+  int nsteps;
+  int smem_bytes;
+};
+
+// Per-CTA PT workspace: four FP64 complex matrices (working matrix, U,
+// carry, theta) and one double-float matrix.
+inline long long pt_work_bytes(long long wcap) { return wcap * (4 * 16 + 16); }
+
+cudaError_t launch_pt(const PtLaunch& L, int precision, int grid, int block, cudaStream_t stream);
+
+// ------------------------------------------------------- process-tensor sweep
+
+struct DynLaunch {
+  int nh;             // systems swept together
+  int D;
+  int d;
+  const double* sites;  // PT sites of one instance (complex128, [l][a][r] per slot)
+  long long slot_elems;
+  const int2* dims;     // per step (l, r)
+  const double* caps;   // (num_steps + 1) * cap
+  int cap;
+  const double* p1;     // nh * D * D (eigenbasis-folded)
+  const double* p2;
+  double* vcur;         // nh * cap * D
+  double* vnext;
+  double* out;          // (num_steps + 1) * nh * D
+  int k;                // step
+};
+
+cudaError_t launch_dyn_step(const DynLaunch& L, int r, cudaStream_t stream);
+cudaError_t launch_dyn_init(const DynLaunch& L, const double* rho0, cudaStream_t stream);
 
 }  // namespace otb

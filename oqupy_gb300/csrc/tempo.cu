@@ -385,7 +385,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     if (tid < D) {
       zc acc = mk<double>(0, 0);
       for (int c = 0; c < D; ++c) cfma(acc, P2[tid * D + c], sh.v[cur][c]);
-      b.out[I.out_base + (long long)(step % I.out_cap) * D + tid] = acc;
+      b.out[I.out_base + (long long)((step - I.out_origin) % I.out_cap) * D + tid] = acc;
     }
     if (tid == 0) {
       sh.st.step = step;

@@ -8,9 +8,19 @@ GPU backend when ``backend_config["backend"] == "gb300"`` and the reference
 class otherwise, so existing code selects the GPU path through its existing
 configuration.  The factory dispatches before the reference constructor runs,
 so the reference never sees the unknown backend name.
+
+``compute_dynamics`` has no configuration argument
+(oqupy/system_dynamics.py:41-53): the wrapper routes a call to the GPU sweep
+when its single process tensor was built by the GPU backend (it carries a
+device twin), there is no control and ``record_all`` is set, and otherwise
+calls the reference function.  Both ``oqupy.system_dynamics.compute_dynamics``
+and ``oqupy.compute_dynamics`` (bound at import, oqupy/__init__.py:104) are
+rebound.
 """
 
 from typing import Any, Dict, Optional
+
+import numpy as np
 
 BACKEND_NAME = "gb300"
 _installed: Dict[str, Any] = {}
@@ -42,6 +52,69 @@ def install(oqupy_module: Any = None) -> None:
         tempo_backend.reference_class = ref_cls
         tempo_mod.TempoBackend = tempo_backend
 
+    pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
+    from .pt import GpuPtTempoBackend
+    if "PtTempoBackend" not in _installed:
+        ref_pt = pt_mod.PtTempoBackend
+        _installed["PtTempoBackend"] = ref_pt
+
+        def pt_tempo_backend(*args, config=None, degeneracy_maps=None, **kwargs):
+            if _wants_gpu(config) and degeneracy_maps is None:
+                return GpuPtTempoBackend(*args, config=config, degeneracy_maps=None, **kwargs)
+            if _wants_gpu(config):
+                config = {k: v for k, v in config.items() if k != "backend"}
+            return ref_pt(*args, config=config, degeneracy_maps=degeneracy_maps, **kwargs)
+
+        pt_tempo_backend.reference_class = ref_pt
+        pt_mod.PtTempoBackend = pt_tempo_backend
+
+    sd_mod = importlib.import_module(oqupy_module.__name__ + ".system_dynamics")
+    if "compute_dynamics" not in _installed:
+        ref_cd = sd_mod.compute_dynamics
+        _installed["compute_dynamics"] = ref_cd
+        _installed["compute_dynamics_pkg"] = getattr(oqupy_module, "compute_dynamics", None)
+        sys_mod = importlib.import_module(oqupy_module.__name__ + ".system")
+        dyn_mod = importlib.import_module(oqupy_module.__name__ + ".dynamics")
+
+        def compute_dynamics(system, initial_state=None, dt=None, num_steps=None,
+                             start_time=0.0, process_tensor=None, control=None,
+                             record_all=True, subdiv_limit=None,
+                             liouvillian_epsrel=None, progress_type=None):
+            kwargs = dict(initial_state=initial_state, dt=dt, num_steps=num_steps,
+                          start_time=start_time, process_tensor=process_tensor,
+                          control=control, record_all=record_all,
+                          progress_type=progress_type)
+            if subdiv_limit is not None:
+                kwargs["subdiv_limit"] = subdiv_limit
+            if liouvillian_epsrel is not None:
+                kwargs["liouvillian_epsrel"] = liouvillian_epsrel
+            pts = process_tensor if isinstance(process_tensor, list) else \
+                ([] if process_tensor is None else [process_tensor])
+            gpu = (len(pts) == 1 and hasattr(pts[0], "_gb300") and control is None
+                   and record_all and type(system) is sys_mod.System)
+            if not gpu:
+                return ref_cd(system, **kwargs)
+            parsed = sd_mod._compute_dynamics_input_parse(
+                False, system, initial_state, dt, num_steps, start_time,
+                process_tensor, control, record_all)
+            system, initial_state, dt, num_steps, start_time = parsed[:5]
+            hs_dim = parsed[-1]
+            args = [dt, start_time]
+            args.append(kwargs.get("subdiv_limit", sd_mod.SUBDIV_LIMIT))
+            args.append(kwargs.get("liouvillian_epsrel", sd_mod.INTEGRATE_EPSREL))
+            p1, p2 = system.get_propagators(*args)(0)
+            from .pt import device_compute_dynamics
+            st = device_compute_dynamics(pts[0], [(p1, p2)],
+                                         [initial_state.reshape(-1)], num_steps)
+            states = [s.reshape(hs_dim, hs_dim) for s in st[:, 0]]
+            times = start_time + np.arange(len(states)) * dt
+            return dyn_mod.Dynamics(times=list(times), states=states)
+
+        compute_dynamics.reference_function = ref_cd
+        sd_mod.compute_dynamics = compute_dynamics
+        if _installed["compute_dynamics_pkg"] is not None:
+            oqupy_module.compute_dynamics = compute_dynamics
+
 
 def uninstall(oqupy_module: Any = None) -> None:
     if oqupy_module is None:
@@ -50,3 +123,12 @@ def uninstall(oqupy_module: Any = None) -> None:
     tempo_mod = importlib.import_module(oqupy_module.__name__ + ".tempo")
     if "TempoBackend" in _installed:
         tempo_mod.TempoBackend = _installed.pop("TempoBackend")
+    if "PtTempoBackend" in _installed:
+        pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
+        pt_mod.PtTempoBackend = _installed.pop("PtTempoBackend")
+    if "compute_dynamics" in _installed:
+        sd_mod = importlib.import_module(oqupy_module.__name__ + ".system_dynamics")
+        sd_mod.compute_dynamics = _installed.pop("compute_dynamics")
+        pkg = _installed.pop("compute_dynamics_pkg", None)
+        if pkg is not None:
+            oqupy_module.compute_dynamics = pkg

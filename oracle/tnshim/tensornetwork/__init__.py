@@ -12,7 +12,8 @@ touches:
   ``shape``, ``get_rank``, ``reorder_edges``, ``get_all_dangling``)
 * ``Edge`` (``__xor__`` = connect, ``dimension``, ``disconnect``)
 * ``contract``, ``contract_between``, ``copy``, ``contractors.greedy``
-* ``split_node_full_svd`` with the relative / absolute truncation rule:
+* ``split_node_full_svd`` (numpy's LAPACK gesdd; ``OQUPY_TNSHIM_SVD=gesvd``
+  selects LAPACK gesvd) with the relative / absolute truncation rule:
   discard the longest tail of singular values whose 2-norm is
   ``<= max_truncation_err`` (times ``s[0]`` when ``relative``).  The same rule
   is stated inside the reference at ``oqupy/mps_mpo.py:452-457``.
@@ -20,6 +21,7 @@ touches:
 Nothing in the product package may import this module.
 """
 
+import os
 from typing import Any, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -258,7 +260,14 @@ def split_node_full_svd(
     m = int(np.prod(lshape)) if lshape else 1
     n = int(np.prod(rshape)) if rshape else 1
     mat = t.reshape(m, n)
-    u, s, vh = np.linalg.svd(mat, full_matrices=False)
+    if os.environ.get("OQUPY_TNSHIM_SVD", "gesdd") == "gesvd":
+        # LAPACK's QR-iteration driver instead of divide-and-conquer: used
+        # only to measure how much the reference's own result depends on
+        # which (equally valid) SVD algorithm it calls
+        import scipy.linalg
+        u, s, vh = scipy.linalg.svd(mat, full_matrices=False, lapack_driver="gesvd")
+    else:
+        u, s, vh = np.linalg.svd(mat, full_matrices=False)
     if max_singular_values is None:
         max_singular_values = s.size
     if max_truncation_err is not None:

@@ -11,7 +11,10 @@ calls on this path.  For every case the script records the exact inputs the
 reference backend consumed (influence matrices per ``dk``, half-step
 propagators, coupling unitary, initial state) and the reference's outputs
 (density matrix per step, bond dimensions), so the oracle and the CUDA path
-can be run on bit-identical inputs.  Process tensors are gauge dependent and
+can be run on bit-identical inputs.  Each case also records a per-step
+rounding envelope: how far the unmodified reference itself moves when its
+inputs are perturbed by 1e-15 relative (two seeds) or when its SVD calls use
+LAPACK gesvd instead of gesdd.  Process tensors are gauge dependent and
 are not stored; their bond dimensions and the dynamics computed from them are.
 """
 
@@ -188,11 +191,17 @@ def run_case(oqupy, name, c):
                    for s in range(c["dkmax"] + 1, nsteps + 1)]
             out["tempo_infl_neg"] = np.array(neg)
         env = np.zeros(nsteps + 1)
-        for seed in (1, 2):
+        for seed in (1, 2, "gesvd"):
             t2 = oqupy.Tempo(sys_objs[0], bath, params, c["rho0"], 0.0)
-            t2._backend_instance._influence = _perturbed(
-                t2._backend_instance._influence, seed)
-            dyn2 = t2.compute(end_time, progress_type="silent")
+            if seed == "gesvd":
+                os.environ["OQUPY_TNSHIM_SVD"] = "gesvd"
+            else:
+                t2._backend_instance._influence = _perturbed(
+                    t2._backend_instance._influence, seed)
+            try:
+                dyn2 = t2.compute(end_time, progress_type="silent")
+            finally:
+                os.environ.pop("OQUPY_TNSHIM_SVD", None)
             st2 = np.array(dyn2.states).reshape(-1, d * d)
             env = np.maximum(env, [_trace_dist(a, b) for a, b in
                                    zip(out["tempo_states"], st2)])
@@ -219,11 +228,17 @@ def run_case(oqupy, name, c):
             out["pt_transform_in"] = pt.transform_in
             out["pt_transform_out"] = pt.transform_out
         env = np.zeros(out["pt_states"].shape[:2])
-        for seed in (1, 2):
+        for seed in (1, 2, "gesvd"):
             p2 = oqupy.PtTempo(bath, 0.0, end_time, params)
-            p2._backend_instance._influence = _perturbed(
-                p2._backend_instance._influence, seed)
-            pt2 = p2.get_process_tensor(progress_type="silent")
+            if seed == "gesvd":
+                os.environ["OQUPY_TNSHIM_SVD"] = "gesvd"
+            else:
+                p2._backend_instance._influence = _perturbed(
+                    p2._backend_instance._influence, seed)
+            try:
+                pt2 = p2.get_process_tensor(progress_type="silent")
+            finally:
+                os.environ.pop("OQUPY_TNSHIM_SVD", None)
             for i, s in enumerate(sys_objs):
                 dyn = oqupy.compute_dynamics(system=s, process_tensor=pt2,
                                              initial_state=c["rho0"],
