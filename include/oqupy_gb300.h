@@ -186,6 +186,49 @@ otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t n_systems,
                        const double* rho0, int32_t num_steps, double* out,
                        void* stream);
 
+/* ----------------------------------------------- allocation-free TEMPO */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory through this library -- a host framework whose memory pool owns
+ * every device allocation, or code running where cudaMalloc is not allowed:
+ * the caller allocates all device buffers below, and the TEMPO step's
+ * working memory comes from a fixed device array inside the library
+ * (1 MiB, present on every GPU that loads the library until exit), which
+ * limits bonds to chi_cap * D <= OTB_TEMPO_STATIC_MAX_CHI_D.
+ *
+ * One instance, one CTA.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should therefore come before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race, so issue them on one stream (or otherwise serialise them).  Nothing
+ * in the array needs to start at zero.  The MPS buffer must be zeroed by the
+ * caller before the first call; it then carries the instance between calls.
+ * The function calls no cudaMalloc or cudaFree. */
+#define OTB_TEMPO_STATIC_MAX_CHI_D 128
+/* bytes of the MPS buffer: state header, dims, (dkmax+2) site slots */
+#define OTB_TEMPO_STATIC_MPS_BYTES(hs_dim, dkmax, chi_cap)                          \
+  (256LL + ((((long long)(dkmax) + 2) * 8 + 255) / 256) * 256 +                     \
+   ((long long)(dkmax) + 2) * (long long)(chi_cap) * (hs_dim) * (hs_dim) *          \
+       (long long)(chi_cap) * 16)
+
+typedef struct {
+  int32_t hs_dim;            /* d (D = d*d) */
+  int32_t dkmax;             /* memory length (>= 0) */
+  double epsrel;
+  int32_t chi_cap;           /* bond capacity, chi_cap * D <= 128 */
+  int32_t precision;         /* OTB_PRECISION_* */
+  const double* influences;  /* device: (dkmax+1) * D * D complex, as otb_tempo_instance */
+  const double* props;       /* device: P1 then P2 (eigenbasis-folded), 2 * D * D complex */
+  const double* rho0;        /* device: D complex (read on the first call) */
+  void* mps;                 /* device: OTB_TEMPO_STATIC_MPS_BYTES bytes, zeroed before
+                                the first call */
+  int64_t mps_bytes;
+  double* states_out;        /* device: nsteps * D complex, states of this call's steps */
+} otb_tempo_static_io;
+
+/* Advance one TEMPO instance by nsteps without allocating. */
+otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, int32_t nsteps,
+                                    void* stream);
+
 /* Measured FMA-pipe throughput of this GPU (TFLOP/s, 2 flops per FMA):
  * precision 0 = FP64 (DFMA), 1 = FP32 (FFMA).  Used as the roofline peak of
  * the Jacobi kernels, which run on these pipes. */

@@ -28,6 +28,12 @@
 // bond split (jacobi.cuh).
 #include <math.h>
 
+#include <cmath>
+#include <mutex>
+
+#include "../../include/oqupy_gb300.h"
+#include "capi_util.h"
+
 #include "engine.h"
 #include "jacobi.cuh"
 
@@ -463,4 +469,154 @@ cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int bloc
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free single-instance entry point
+// ---------------------------------------------------------------------------
+//
+// Callers that cannot allocate device memory themselves through the library
+// (a host framework that owns every device allocation through its own pool,
+// or code running where cudaMalloc is not allowed) pass all device buffers in
+// and get the TEMPO step's working memory from this file-scope array.  It is
+// one CTA's workspace for splits of at most (chi_cap * D) columns with
+// chi_cap * D <= 128: 128 * 128 * 64 bytes = 1 MiB, held by every GPU that
+// loads the library until the process exits.  No part of it has to start at
+// zero: every workspace matrix is written before it is read.
+constexpr int STATIC_MAX_CHI_D = 128;
+constexpr long long STATIC_WCAP = (long long)STATIC_MAX_CHI_D * STATIC_MAX_CHI_D;
+constexpr long long STATIC_SCRATCH_BYTES = STATIC_WCAP * (3 * 16 + 16);
+static __device__ __align__(256) unsigned char g_tempo_static_scratch[STATIC_SCRATCH_BYTES];
+
+template <bool MIXED>
+__global__ void __launch_bounds__(TEMPO_THREADS)
+    tempo_static_kernel(TempoLaunch L, InstDev I, const double* rho0, int nsteps) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ SharedStep sh;
+  Bufs b;
+  b.sites = (zc*)L.sites;
+  b.dims = L.dims;
+  b.infl = (const zc*)L.infl;
+  b.props = (const zc*)L.props;
+  b.out = (zc*)L.out;
+  b.Wg = (zc*)L.work;
+  b.Tg = b.Wg + L.wcap;
+  b.Cg = b.Tg + L.wcap;
+  b.Wffg = (cff*)(b.Cg + L.wcap);
+  b.smem = dsm;
+  b.smem_bytes = L.smem_bytes;
+  const int tid = threadIdx.x;
+  if (tid == 0) sh.st = L.state[0];
+  __syncthreads();
+  if (sh.st.step == 0 && sh.st.nsites == 0) {
+    // first call on a zeroed MPS buffer: the initial state as a (1, D, 1) site
+    for (int a = tid; a < I.D; a += blockDim.x) b.sites[a] = ((const zc*)rho0)[a];
+    if (tid == 0) {
+      b.dims[0] = make_int2(1, 1);
+      sh.st.nsites = 1;
+      sh.st.head = 0;
+      sh.st.status = ST_OK;
+      L.state[0] = sh.st;
+    }
+    __syncthreads();
+  }
+  I.out_origin = sh.st.step + 1;  // states of this call fill out[0 .. nsteps)
+  __syncthreads();
+  for (int s = 0; s < nsteps; ++s) {
+    tempo_step<MIXED>(L, I, 0, b, sh);
+    __syncthreads();
+    if (sh.st.status != ST_OK) break;
+  }
+}
+
 }  // namespace otb
+
+namespace {
+
+std::mutex g_static_mutex;
+void* g_static_addr[64];
+bool g_static_ready[64];
+
+}  // namespace
+
+extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, int32_t nsteps,
+                                               void* stream) {
+  using namespace otb;
+  if (!io) return set_error(OTB_ERR_INVALID_ARG, "null io");
+  if (io->hs_dim < 1 || io->hs_dim > 3) return set_error(OTB_ERR_INVALID_ARG, "hs_dim must be 1..3");
+  const int D = io->hs_dim * io->hs_dim;
+  if (io->chi_cap < D) return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be >= D");
+  if ((long long)io->chi_cap * D > STATIC_MAX_CHI_D)
+    return set_error(OTB_ERR_INVALID_ARG,
+                     "chi_cap * D exceeds the static scratch of otb_tempo_advance_static "
+                     "(chi_cap * D <= 128; use otb_tempo_create/advance for larger bonds)");
+  if (io->dkmax < 0) return set_error(OTB_ERR_INVALID_ARG, "dkmax must be >= 0 (no full memory)");
+  if (!(io->epsrel > 0.0) || !std::isfinite(io->epsrel))
+    return set_error(OTB_ERR_INVALID_ARG, "epsrel must be positive and finite");
+  if (io->precision != 0 && io->precision != 1)
+    return set_error(OTB_ERR_INVALID_ARG, "precision must be 0 (complex128) or 1 (mixed)");
+  if (!io->influences || !io->props || !io->rho0 || !io->mps || !io->states_out)
+    return set_error(OTB_ERR_INVALID_ARG, "null device buffer");
+  if (nsteps < 1) return set_error(OTB_ERR_INVALID_ARG, "nsteps must be >= 1");
+  if (io->mps_bytes < (int64_t)OTB_TEMPO_STATIC_MPS_BYTES(io->hs_dim, io->dkmax, io->chi_cap))
+    return set_error(OTB_ERR_INVALID_ARG, "mps buffer smaller than OTB_TEMPO_STATIC_MPS_BYTES");
+  int dev = 0;
+  if (!check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return OTB_ERR_CUDA;
+  if (dev < 0 || dev >= 64) return set_error(OTB_ERR_INVALID_ARG, "device index out of range");
+  {
+    // once per device, with that device current: the scratch array's device
+    // address (the symbol name is only a host-side stand-in)
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_ready[dev]) {
+      void* p = nullptr;
+      if (!check_cuda(cudaGetSymbolAddress(&p, g_tempo_static_scratch), "cudaGetSymbolAddress"))
+        return OTB_ERR_CUDA;
+      g_static_addr[dev] = p;
+      g_static_ready[dev] = true;
+    }
+  }
+  const int nslots = io->dkmax + 2;
+  unsigned char* mps = (unsigned char*)io->mps;
+  InstDev I;
+  I.D = D;
+  I.dkmax = io->dkmax;
+  I.cap = io->chi_cap;
+  I.nslots = nslots;
+  I.epsrel = io->epsrel;
+  I.site_base = 0;
+  I.dims_base = 0;
+  I.infl_base = 0;
+  I.ninfl = io->dkmax + 1;
+  I.out_cap = nsteps;
+  I.prop_base = 0;
+  I.out_base = 0;
+  I.ovr_base = 0;
+  I.out_origin = 0;
+  TempoLaunch L;
+  L.n = 1;
+  L.inst = nullptr;
+  L.state = (InstState*)mps;
+  L.dims = (int2*)(mps + 256);
+  L.sites = mps + 256 + (((size_t)nslots * sizeof(int2) + 255) / 256) * 256;
+  L.infl = io->influences;
+  L.props = io->props;
+  L.out = io->states_out;
+  L.work = g_static_addr[dev];
+  L.work_stride = 0;
+  L.wcap = (long long)(io->chi_cap * D) * (io->chi_cap * D);
+  L.queue = nullptr;
+  L.order = nullptr;
+  L.nsteps = nsteps;
+  const int smem = tempo_smem_bytes(io->precision);
+  L.smem_bytes = smem;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (io->precision == 0) {
+    e = cudaFuncSetAttribute(tempo_static_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) tempo_static_kernel<false><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps);
+  } else {
+    e = cudaFuncSetAttribute(tempo_static_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) tempo_static_kernel<true><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (!check_cuda(e, "otb_tempo_advance_static launch")) return OTB_ERR_CUDA;
+  return OTB_OK;
+}
