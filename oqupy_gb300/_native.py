@@ -40,7 +40,8 @@ c_int32_p = ctypes.POINTER(ctypes.c_int32)
 
 class TempoConfig(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("chi_cap", ctypes.c_int32),
-                ("out_cap", ctypes.c_int32), ("grid", ctypes.c_int32)]
+                ("out_cap", ctypes.c_int32), ("grid", ctypes.c_int32),
+                ("block", ctypes.c_int32), ("smem_kb", ctypes.c_int32)]
 
 
 class TempoInstance(ctypes.Structure):

@@ -1,0 +1,73 @@
+"""Launch-shape autotuner for the batched TEMPO kernel.
+
+The bond splits of one instance run on one CTA, so the free parameters are
+the CTA width, how many CTAs share an SM and how much shared memory each gets
+for working matrices (matrices that do not fit stay in global memory behind
+L1/L2).  The best choice depends on the bond dimensions of the batch.
+``tune`` times each candidate shape on a sample of the batch for a few steps
+from the start and returns the fastest; results can be cached per
+(D, dkmax bucket) in a JSON file.
+"""
+
+import json
+import os
+import time
+from typing import Dict, List, Optional, Sequence, Tuple
+
+from .tempo import TempoBatch
+
+# (threads per CTA, CTAs per SM, dynamic smem KiB)
+CANDIDATES: List[Tuple[int, int, int]] = [
+    (256, 3, 56), (256, 2, 88), (256, 1, 200), (192, 3, 56), (128, 4, 48)]
+
+
+def _sm_count() -> int:
+    try:
+        import torch
+        return torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        return 152
+
+
+def bucket(instances: Sequence[Dict]) -> str:
+    D = max(int(i["hs_dim"]) ** 2 for i in instances)
+    dk = max(int(i["dkmax"]) if i.get("dkmax") is not None else 10 ** 6 for i in instances)
+    return f"D{D}-dk{min(dk, 1000) // 50 * 50}"
+
+
+def tune(instances: Sequence[Dict], precision: str = "mixed", steps: int = 12,
+         sample: int = 0, candidates: Optional[Sequence[Tuple[int, int, int]]] = None,
+         cache: Optional[str] = None) -> Dict:
+    """Return ``{"block", "ctas_per_sm", "smem_kb", "timings"}`` for the
+    fastest candidate on ``instances`` (or a sample of them)."""
+    key = f"{precision}:{bucket(instances)}"
+    if cache and os.path.exists(cache):
+        table = json.load(open(cache))
+        if key in table:
+            return table[key]
+    cands = list(candidates or CANDIDATES)
+    insts = list(instances)
+    if sample and sample < len(insts):
+        stride = len(insts) / sample
+        insts = [insts[int(k * stride)] for k in range(sample)]
+    sms = _sm_count()
+    timings = []
+    for block, per_sm, smem in cands:
+        b = TempoBatch(insts, precision=precision, out_cap=2, block=block, smem_kb=smem,
+                       grid=min(len(insts), per_sm * sms))
+        t0 = time.perf_counter()
+        b.advance(steps)
+        b.info(0)                      # synchronises
+        dt = time.perf_counter() - t0
+        b.check_status()
+        b.close()
+        timings.append(((block, per_sm, smem), dt))
+    (block, per_sm, smem), _ = min(timings, key=lambda x: x[1])
+    res = {"block": block, "ctas_per_sm": per_sm, "smem_kb": smem,
+           "timings": [[list(c), t] for c, t in timings]}
+    if cache:
+        table = json.load(open(cache)) if os.path.exists(cache) else {}
+        table[key] = res
+        with open(cache, "w") as f:
+            json.dump(table, f, indent=1)
+    return res

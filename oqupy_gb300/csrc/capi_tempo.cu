@@ -20,6 +20,7 @@ struct otb_tempo {
   int out_cap = 0;
   int grid = 0;
   int block = 256;
+  int smem_bytes = 0;
   int Dmax = 0;
   size_t elem = 16;  // bytes per site element (complex128 in both forms)
   std::vector<InstDev> inst;
@@ -136,7 +137,13 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   if (cfg->chi_cap < 4 || cfg->chi_cap > 128)
     return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be in [4, 128]");
   if (cfg->out_cap < 2) return set_error(OTB_ERR_INVALID_ARG, "out_cap must be >= 2");
+  if (cfg->block != 0 && (cfg->block < 64 || cfg->block > 256 || cfg->block % 32 != 0))
+    return set_error(OTB_ERR_INVALID_ARG, "block must be 0 or a multiple of 32 in [64, 256]");
+  if (cfg->smem_kb < 0 || cfg->smem_kb > 200)
+    return set_error(OTB_ERR_INVALID_ARG, "smem_kb must be in [0, 200]");
   std::unique_ptr<otb_tempo> h(new otb_tempo());
+  h->block = cfg->block > 0 ? cfg->block : 256;
+  h->smem_bytes = cfg->smem_kb * 1024;
   h->n = n;
   h->precision = cfg->precision;
   h->cap = cfg->chi_cap;
@@ -251,7 +258,10 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, 2 * std::max(sms, 1)));
+  // default launch shape (measured best of the shapes the autotuner tries on
+  // the batched configuration): 3 CTAs of 256 threads per SM, 56 KiB smem
+  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, 3 * std::max(sms, 1)));
+  if (h->smem_bytes == 0) h->smem_bytes = 56 * 1024;
   h->wcap = (long long)(h->cap * h->Dmax) * (h->cap * h->Dmax);
   h->work_stride = tempo_work_bytes(h->wcap);
   if (!h->d_work.alloc((size_t)h->grid * h->work_stride)) return OTB_ERR_OOM;
@@ -297,7 +307,7 @@ extern "C" otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stre
   L.order = (const int*)h->d_order.p;
   L.nsteps = nsteps;
   L.smem_bytes = 0;
-  if (!check_cuda(launch_tempo(L, h->precision, h->grid, h->block, s), "tempo launch"))
+  if (!check_cuda(launch_tempo(L, h->precision, h->grid, h->block, h->smem_bytes, s), "tempo launch"))
     return OTB_ERR_CUDA;
   return OTB_OK;
 }

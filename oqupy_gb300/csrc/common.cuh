@@ -6,8 +6,9 @@
 
 namespace otb {
 
+// aligned to its size so that an element is one vector load / store
 template <typename T>
-struct cx {
+struct __align__(2 * sizeof(T)) cx {
   T x, y;
 };
 

@@ -65,7 +65,7 @@ inline long long tempo_work_bytes(long long wcap) { return wcap * (3 * 16 + 16);
 // on the FP32 pipe; FP64 sites, contractions, rotation angles, norms, rank
 // decisions and read-out)
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
-                         cudaStream_t stream);
+                         int smem_bytes, cudaStream_t stream);
 int tempo_smem_bytes(int precision);
 
 // ---------------------------------------------------------------- PT-TEMPO

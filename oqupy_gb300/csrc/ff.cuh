@@ -65,8 +65,8 @@ __device__ __forceinline__ ff ff_shfl_xor(ff v, int off) {
   return ff_make(__shfl_xor_sync(0xffffffffu, v.hi, off, 32), __shfl_xor_sync(0xffffffffu, v.lo, off, 32));
 }
 
-// complex double-float
-struct cff {
+// complex double-float (16 bytes, one vector load)
+struct __align__(16) cff {
   ff x, y;
 };
 

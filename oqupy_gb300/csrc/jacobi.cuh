@@ -32,6 +32,8 @@ constexpr int JACOBI_MAX_SWEEPS = 60;
 struct JacobiShared {
   double red[33];
   int flag[2];
+  float worst[2];   // largest relative off-diagonal rotated in a sweep
+  int noise_converged;
   int kept;
   int status;
   int sweeps;     // FP64 sweeps of the last split
@@ -69,7 +71,11 @@ __device__ int jacobi_sweeps(cx<T>* W, int m, int n, int ld, cx<T>* V, int ldv, 
   const int nn = np << 1;
   const T tol = tol_scale * sqrt((T)m) * num<T>::eps();
   const T bigz = num<T>::big_zeta();
-  if (tid == 0) sh->flag[0] = 0;
+  if (tid == 0) {
+    sh->flag[0] = 0;
+    sh->worst[0] = 0.f;
+    sh->noise_converged = 0;
+  }
   __syncthreads();
   if (n <= 1) return 0;
   int sweep;
@@ -157,6 +163,10 @@ __device__ int jacobi_sweeps(cx<T>* W, int m, int n, int ld, cx<T>* V, int ldv, 
               ca[r] = nu;
               cb[r] = nv;
             }
+            if (lane == 0) {
+              const float ratio = (float)(g / (sqrt(al) * sqrt(be)));
+              atomicMax((int*)&sh->worst[sweep & 1], __float_as_int(ratio));
+            }
             if (V != nullptr) {
               cx<T>* va = V + (size_t)a * ldv;
               cx<T>* vb = V + (size_t)b * ldv;
@@ -179,9 +189,15 @@ __device__ int jacobi_sweeps(cx<T>* W, int m, int n, int ld, cx<T>* V, int ldv, 
       __syncthreads();
     }
     const int rotated = sh->flag[sweep & 1];
-    if (tid == 0) sh->flag[(sweep + 1) & 1] = 0;
+    const float worst = sh->worst[sweep & 1];
+    if (tid == 0) {
+      sh->flag[(sweep + 1) & 1] = 0;
+      sh->worst[(sweep + 1) & 1] = 0.f;
+    }
     __syncthreads();
     if (!rotated) break;
+    // at the sweep cap, rotations below 1e-10 relative are rounding noise
+    if (sweep == max_sweeps - 1 && worst < 1e-10f && tid == 0) sh->noise_converged = 1;
   }
   return sweep;
 }
@@ -201,8 +217,14 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
   const int np = (n + 1) >> 1;
   const int nn = np << 1;
   const float eps_ff = 3.6e-15f;  // ~2^-48, double-float unit roundoff
-  const float tol = sqrtf((float)m) * eps_ff;
-  if (tid == 0) sh->flag[0] = 0;
+  // the sloppy FF add and accumulated dot products sit a few units above
+  // eps_ff: stopping test at 4x and numerical-zero floor at 32x
+  const float tol = 4.f * sqrtf((float)m) * eps_ff;
+  if (tid == 0) {
+    sh->flag[0] = 0;
+    sh->worst[0] = 0.f;
+    sh->noise_converged = 0;
+  }
   __syncthreads();
   if (n <= 1) return 0;
   int sweep;
@@ -227,7 +249,7 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
         sh->red[32] = v;
       }
       __syncthreads();
-      const float zf = 16.f * sqrtf((float)m) * eps_ff;
+      const float zf = 32.f * sqrtf((float)m) * eps_ff;
       zfloor = zf * zf * (float)sh->red[32];
     }
     for (int round = 0; round < nn - 1; ++round) {
@@ -247,22 +269,25 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
           b = t;
         }
         const bool active = (p < np) && (b < n);
-        ff al = ff_make(0.f, 0.f), be = al, gr = al, gi = al;
+        // squared norms only steer the angle and the thresholds: FP32 from
+        // the high parts; the off-diagonal gamma decides convergence: FF
+        float A = 0.f, B = 0.f;
+        ff gr = ff_make(0.f, 0.f), gi = gr;
         cff* ca = W + (size_t)a * ld;
         cff* cb = W + (size_t)b * ld;
         if (active) {
           for (int r = lane; r < m; r += G) {
             const cff u = ca[r];
             const cff v = cb[r];
-            al = ff_fma(u.x, u.x, ff_fma(u.y, u.y, al));
-            be = ff_fma(v.x, v.x, ff_fma(v.y, v.y, be));
+            A = fmaf(u.x.hi, u.x.hi, fmaf(u.y.hi, u.y.hi, A));
+            B = fmaf(v.x.hi, v.x.hi, fmaf(v.y.hi, v.y.hi, B));
             gr = ff_fma(u.x, v.x, ff_fma(u.y, v.y, gr));
             gi = ff_fma(u.x, v.y, ff_sub(gi, ff_mul(u.y, v.x)));
           }
         }
         for (int off = G >> 1; off > 0; off >>= 1) {
-          al = ff_add(al, ff_shfl_xor(al, off));
-          be = ff_add(be, ff_shfl_xor(be, off));
+          A += __shfl_xor_sync(0xffffffffu, A, off, 32);
+          B += __shfl_xor_sync(0xffffffffu, B, off, 32);
           gr = ff_add(gr, ff_shfl_xor(gr, off));
           gi = ff_add(gi, ff_shfl_xor(gi, off));
         }
@@ -271,7 +296,6 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
           // accuracy (later sweeps correct it); unitarity is what must hold to
           // FF precision, so c, s come from t through an FF rsqrt
           // (c^2 + s^2 = c^2 (1 + t^2) = 1) and the phase is normalised in FF.
-          const float A = al.hi, B = be.hi;
           const float g = hypotf(gr.hi, gi.hi);
           if (A > zfloor && B > zfloor && g > tol * sqrtf(A) * sqrtf(B)) {
             const float zeta = (B - A) / (2.f * g);
@@ -302,16 +326,25 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
               ca[r] = nu;
               cb[r] = nv;
             }
-            if (lane == 0) sh->flag[sweep & 1] = 1;
+            if (lane == 0) {
+              sh->flag[sweep & 1] = 1;
+              atomicMax((int*)&sh->worst[sweep & 1], __float_as_int(g / (sqrtf(A) * sqrtf(B))));
+            }
           }
         }
       }
       __syncthreads();
     }
     const int rotated = sh->flag[sweep & 1];
-    if (tid == 0) sh->flag[(sweep + 1) & 1] = 0;
+    const float worst = sh->worst[sweep & 1];
+    if (tid == 0) {
+      sh->flag[(sweep + 1) & 1] = 0;
+      sh->worst[(sweep + 1) & 1] = 0.f;
+    }
     __syncthreads();
     if (!rotated) break;
+    // at the sweep cap, rotations below 1e-10 relative are rounding noise
+    if (sweep == JACOBI_MAX_SWEEPS - 1 && worst < 1e-10f && tid == 0) sh->noise_converged = 1;
   }
   return sweep;
 }
@@ -361,7 +394,7 @@ __device__ int jacobi_finish(const cx<T>* W, int m, int n, int ld, double epsrel
     sh->status = ST_OK;
     if (!finite)
       sh->status = ST_NONFINITE;
-    else if (sweeps >= JACOBI_MAX_SWEEPS)
+    else if (sweeps >= JACOBI_MAX_SWEEPS && !sh->noise_converged)
       sh->status = ST_NO_CONVERGENCE;
   }
   __syncthreads();
@@ -400,10 +433,17 @@ __device__ inline int jacobi_truncate_mixed(cx<double>* W, int m, int n, cff* Wf
   for (int idx = tid; idx < m * n; idx += nt) Wff[idx] = cff_from(cscale(W[idx], inv));
   __syncthreads();
   const int sw = jacobi_sweeps_ff(Wff, m, n, m, sh);
+  const bool ff_done = sw < JACOBI_MAX_SWEEPS || sh->noise_converged;
   for (int idx = tid; idx < m * n; idx += nt) W[idx] = cscale(cff_to(Wff[idx]), scale);
   __syncthreads();
+  // FP64 fallback: if the double-float sweeps did not settle, finish the
+  // (nearly orthogonal) matrix with FP64 sweeps; their count is reported
+  const int sw64 = ff_done ? 0 : jacobi_sweeps<double>(W, m, n, m, nullptr, 0, sh);
   if (threadIdx.x == 0) sh->sweeps32 = sw;
-  return jacobi_finish<double>(W, m, n, m, epsrel, norm, perm, sh, sw);
+  const int kk = jacobi_finish<double>(W, m, n, m, epsrel, norm, perm, sh, ff_done ? 0 : sw64);
+  if (threadIdx.x == 0) sh->sweeps = ff_done ? 0 : sw64;
+  __syncthreads();
+  return kk;
 }
 
 }  // namespace otb

@@ -63,7 +63,7 @@ __device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap,
   __syncthreads();
   const int kk = MIXED ? jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh)
                        : jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
-  *sweeps64 += MIXED ? 0 : sh.jsh.sweeps;
+  *sweeps64 += sh.jsh.sweeps;  // mixed form: FP64 fallback sweeps only
   *sweepsff += MIXED ? sh.jsh.sweeps32 : 0;
   *flops += 4.0 * (6.0 * R * (double)N * N + 20.0 * (double)N * N * N);
   if (sh.jsh.status != ST_OK || kk > cap) {

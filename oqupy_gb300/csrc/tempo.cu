@@ -226,7 +226,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       flops += 8.0 * m * n * ccd + 4.0 * (6.0 * R * N * N + 20.0 * N * N * N);
     }
     ++splits;
-    sw64 += sh.jsh.sweeps;
+    sw64 += sh.jsh.sweeps;   // mixed form: FP64 fallback sweeps only
     sw32 += sh.jsh.sweeps32;
     if (sh.jsh.status != ST_OK || kk > cap) {
       if (tid == 0) sh.st.status = (sh.jsh.status != ST_OK) ? sh.jsh.status : ST_CHI_OVERFLOW;
@@ -451,8 +451,8 @@ int tempo_smem_bytes(int precision) {
 }
 
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
-                         cudaStream_t stream) {
-  const int smem = tempo_smem_bytes(precision);
+                         int smem_bytes, cudaStream_t stream) {
+  const int smem = smem_bytes > 0 ? smem_bytes : tempo_smem_bytes(precision);
   TempoLaunch l2 = L;
   l2.smem_bytes = smem;
   if (precision == 0) {

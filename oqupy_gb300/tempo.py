@@ -60,7 +60,7 @@ class TempoBatch:
 
     def __init__(self, instances: Sequence[Dict], precision: str = "complex128",
                  chi_cap: int = DEFAULT_CHI_CAP, out_cap: int = 2, grid: int = 0,
-                 max_sites: int = 0):
+                 max_sites: int = 0, block: int = 0, smem_kb: int = 0):
         L = nat.lib()
         if precision not in nat.PRECISION:
             raise ValueError(f"precision must be one of {list(nat.PRECISION)}")
@@ -92,7 +92,7 @@ class TempoBatch:
             arr[i].max_sites = int(max_sites)
             self.D.append(D)
         cfg = nat.TempoConfig(nat.PRECISION[precision], int(chi_cap),
-                              int(out_cap), int(grid))
+                              int(out_cap), int(grid), int(block), int(smem_kb))
         self.out_cap = int(out_cap)
         self.chi_cap = int(chi_cap)
         h = ctypes.c_void_p()
