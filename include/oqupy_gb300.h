@@ -232,6 +232,37 @@ typedef struct {
 otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, int32_t nsteps,
                                     void* stream);
 
+/* -------------------------------------------------- MLP surrogate kernels */
+
+/* No counterpart in the reference (the learned screening part of this
+ * project).  All pointers are device pointers owned by the caller; bf16
+ * matrices are row-major with K contiguous.
+ *
+ * C[M][N] = A[M][K] B[N][K]^T on the 5th-generation tensor cores (tcgen05,
+ * bf16 in, FP32 accumulate in TMEM), fused epilogue:
+ *   0: out = C (+ bias)       1: z = C + bias -> z_out, out = gelu(z)
+ *   2: out = C * gelu'(z_in)
+ * out_f32 and/or out_bf16 receive the result; *err is set to 1 if a
+ * bounded wait on the tensor-core completion barrier timed out. */
+otb_status otb_mlp_gemm(const void* A, const void* B, int32_t M, int32_t N, int32_t K,
+                        const float* bias, int32_t epilogue, const float* z_in,
+                        float* z_out, float* out_f32, void* out_bf16, int32_t* err,
+                        void* stream);
+/* out[C][R] = in[R][C] (bf16) */
+otb_status otb_mlp_transpose_bf16(const void* in, void* out, int32_t R, int32_t C,
+                                  void* stream);
+otb_status otb_mlp_f32_to_bf16(const float* in, void* out, int64_t n, void* stream);
+/* out[c] = sum_r in[r][c] (FP32) */
+otb_status otb_mlp_colsum(const float* in, float* out, int32_t R, int32_t C, void* stream);
+/* g = 2 (y - t) / n (FP32 and bf16); *loss += sum (y - t)^2 */
+otb_status otb_mlp_mse_grad(const float* y, const float* t, float* g_f32, void* g_bf16,
+                            int64_t n, double* loss, void* stream);
+/* AdamW step on FP32 master weights (bias-corrected, decoupled weight decay);
+ * refreshes the bf16 copy when w_bf16 is not NULL */
+otb_status otb_mlp_adamw(float* w, const float* g, float* m, float* v, void* w_bf16,
+                         int64_t n, float lr, float beta1, float beta2, float eps,
+                         float weight_decay, int32_t step, void* stream);
+
 /* Measured FMA-pipe throughput of this GPU (TFLOP/s, 2 flops per FMA):
  * precision 0 = FP64 (DFMA), 1 = FP32 (FFMA).  Used as the roofline peak of
  * the Jacobi kernels, which run on these pipes. */
