@@ -223,6 +223,100 @@ def window_sites(insts, first, last):
     return sum(min(s, i["dkmax"] + 1) for i in insts for s in range(first, last + 1))
 
 
+def run_surrogate(args):
+    """Learned-surrogate workload: data from the batched TEMPO solver, GPU
+    training with the tensor-core kernels, calibration, held-out screening
+    with TEMPO fallback above the error budget, and 1e5-point inference.
+    Prints one JSON line; ``value`` = held-out points/s after fallback."""
+    import numpy as np
+    import torch
+    from oqupy_gb300 import surrogate as sg
+    ns, dk = args.sur_steps, args.sur_dkmax
+    t0 = time.perf_counter()
+    P = {k: sg.sample_params(n, seed) for k, n, seed in
+         (("train", args.sur_train, 101), ("val", args.sur_val, 102), ("test", args.sur_test, 103))}
+    Y, tgen = {}, 0.0
+    for k in ("train", "val", "test"):
+        Y[k], t = sg.tempo_bloch(P[k], ns, dkmax=dk)
+        tgen += t
+    ngen = sum(len(v) for v in P.values())
+    sur = sg.Surrogate(nsteps=ns, dkmax=dk, seed=0, bins=args.sur_bins)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    losses = sur.fit(P["train"], Y["train"], epochs=args.sur_epochs, batch=256)
+    torch.cuda.synchronize()
+    ttrain = time.perf_counter() - t1
+    val_err = sur.calibrate(P["val"], Y["val"])
+    clocks = ClockSampler()
+    clocks.start()
+    screens = {}
+    for budget in (1e-3, 1e-2):
+        out, fb, tim = sur.screen(P["test"], budget=budget)
+        err = np.abs(out - Y["test"]).max(axis=(1, 2))
+        screens[f"{budget:g}"] = {
+            "points_per_s": tim["points_per_s"], "fallback_frac": float(fb.mean()),
+            "max_err_after_fallback": float(err.max()),
+            "frac_within_budget": float(np.mean(err <= budget)),
+            "surrogate_s": tim["surrogate_s"], "fallback_s": tim["fallback_s"]}
+
+    # inference throughput: 1e5 in-box points, weights and inputs resident
+    npts = args.sur_points
+    Xp = sur._x(sg.sample_params(npts, 104))
+    for _ in range(3):
+        sur.net.forward(Xp)
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        sur.net.forward(Xp)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    # end to end: host parameters -> device -> forward -> trajectories to host
+    host = sg.sample_params(npts, 105)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        res = sur.predict(host)
+    e2e_s = (time.perf_counter() - te) / args.steps
+    clk = clocks.stop()
+    sizes = sur.net.sizes
+    flops = 2.0 * npts * sum(a * b for a, b in zip(sizes[:-1], sizes[1:]))
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+    achieved = flops / (ms / 1e3) / 1e12
+    scr = screens["0.001"]
+    line = {"metric": "surrogate screening parameter points/s after TEMPO fallback (1e-3 max Bloch error)",
+            "value": scr["points_per_s"], "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 3, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (FP32 accumulate, FP32 master weights)",
+            "data": "synthetic (seeded TEMPO-generated trajectories)",
+            "config": {"workload": f"MLP 5->{sizes[1]}x{len(sizes) - 2} GELU->{sizes[-1]}; "
+                                   f"{args.sur_train} train / {args.sur_val} calibration / "
+                                   f"{args.sur_test} held-out TEMPO trajectories, {ns} steps dt 0.05, "
+                                   f"dkmax {dk}, epsrel 1e-6; H = Omega/2 sx + eps/2 sz",
+                       "error_bins": f"{args.sur_bins}x{args.sur_bins} (alpha x T)",
+                       "l2": "not flushed: inference inputs and weights are the workload's resident state"},
+            "inference": {"points_per_s": npts / (ms / 1e3), "points": npts, "ms": ms},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "tc_gemm_kernel (tcgen05 kind::f16), forward of the MLP",
+                         "peak_source": "measured cuBLAS bf16 burst"},
+            "e2e": {"value": npts / e2e_s, "unit": "points/s (inference only)",
+                    "h2d_bytes_per_step": npts * 5 * 4, "d2h_bytes_per_step": int(res.size * 4)},
+            "screening": screens,
+            "validation_max_err": {"median": float(np.median(val_err)), "p90": float(np.quantile(val_err, 0.9)),
+                                   "max": float(val_err.max())},
+            "err_map": [float(x) for x in sur.err_map],
+            "data_generation": {"trajectories": ngen, "seconds": tgen, "traj_per_s": ngen / tgen},
+            "training": {"epochs": args.sur_epochs, "seconds": ttrain, "loss_first": losses[0],
+                         "loss_last": losses[-1]},
+            "clocks": clk, "gpu_launches": args.steps * (len(sizes) - 1),
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -233,12 +327,30 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--no-complex128", action="store_true")
     ap.add_argument("--chi-cap", type=int, default=64)
+    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate"])
+    ap.add_argument("--sur-train", type=int, default=20000)
+    ap.add_argument("--sur-val", type=int, default=2000)
+    ap.add_argument("--sur-test", type=int, default=2000)
+    ap.add_argument("--sur-steps", type=int, default=500)
+    ap.add_argument("--sur-dkmax", type=int, default=8)
+    ap.add_argument("--sur-epochs", type=int, default=150)
+    ap.add_argument("--sur-bins", type=int, default=4)
+    ap.add_argument("--sur-points", type=int, default=100000)
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     seed = 20261203 + rank
+    if args.workload == "surrogate":
+        if rank != 0:
+            return
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned "
+                              "surrogate; its TEMPO solve is the fallback timed in this workload"}))
+            return
+        run_surrogate(args)
+        return
 
     workload = {"workload": "batched TEMPO spin-boson, 512 instances (alpha U[0.01,0.5], "
                             "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, "
