@@ -67,7 +67,8 @@ def _oracle_worker(args):
     infl = inst["influences"]
     p1, p2 = inst["prop1"], inst["prop2"]
     D = 4
-    o = to.TempoOracle(inst["rho0"].reshape(-1), lambda dk: infl[dk],
+    # negative dk asks for the add_correlation_time influence: none here
+    o = to.TempoOracle(inst["rho0"].reshape(-1), lambda dk: infl[dk] if dk >= 0 else None,
                        inst["unitary"], lambda s: (p1, p2), np.ones(D),
                        np.ones(D), inst["dkmax"], inst["epsrel"])
     o.initialize()

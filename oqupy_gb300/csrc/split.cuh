@@ -61,8 +61,16 @@ __device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap,
     W[idx] = trans ? cconj(X(c, r)) : X(r, c);
   }
   __syncthreads();
-  const int kk = MIXED ? jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh)
-                       : jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
+  // the QR-preconditioned mixed driver returns X^H U (N x kk, ld N) instead of
+  // X V (R x N, ld R): the same two branches below, swapped
+  const bool flip = MIXED && N >= 8;
+  zc* Wr = W;
+  const size_t spare = (size_t)b.smem_bytes > used ? (size_t)b.smem_bytes - used : 0;
+  const int kk = flip ? jacobi_truncate_mixed_qr(W, R, N, Wff, b.smem + used, spare, epsrel, sh.norm,
+                                                 sh.perm, &sh.jsh, &Wr)
+                 : MIXED ? jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh)
+                         : jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
+  W = Wr;
   *sweeps64 += sh.jsh.sweeps;  // mixed form: FP64 fallback sweeps only
   *sweepsff += MIXED ? sh.jsh.sweeps32 : 0;
   *flops += 4.0 * (6.0 * R * (double)N * N + 20.0 * (double)N * N * N);
@@ -71,7 +79,7 @@ __device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap,
     __syncthreads();
     return 0;
   }
-  if (!trans) {
+  if (!(flip ? !trans : trans)) {
     // U = W[:, perm] / s;  C = U^H X
     for (int idx = tid; idx < m * kk; idx += nt) {
       const int j = idx / m, row = idx - j * m;

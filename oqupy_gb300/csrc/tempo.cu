@@ -71,11 +71,15 @@ struct SharedStep {
 // Truncated split of the R x N (R >= N) matrix A = op(src): op is the
 // identity (A(row,c) = src[c*lds+row]) or the conjugate transpose
 // (A(row,c) = conj(src[row*lds+c])).  On return *Wout holds A V (FP64,
-// orthogonal columns, ld R), sh.norm / sh.perm / return value as in
-// jacobi_finish.  Shared memory is used for the working matrices that fit.
+// orthogonal columns, ld R) -- or, when *flip is set (the QR-preconditioned
+// mixed driver), A^H U (FP64, N x kept, ld N) -- with sh.norm / sh.perm /
+// return value as in jacobi_finish.  Shared memory is used for the working
+// matrices that fit.
+constexpr int QR_MIN_COLS = 8;
+
 template <bool MIXED>
 __device__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel,
-                     Bufs& b, SharedStep& sh, zc** Wout) {
+                     Bufs& b, SharedStep& sh, zc** Wout, bool* flip) {
   const int tid = threadIdx.x, nt = blockDim.x;
   size_t used = 0;
   auto take = [&](size_t bytes) -> void* {
@@ -98,6 +102,13 @@ __device__ int split(const zc* src, int lds, bool src_trans, int R, int N, doubl
   }
   __syncthreads();
   int kk;
+  *flip = false;
+  if (MIXED && N >= QR_MIN_COLS) {
+    *flip = true;
+    const size_t spare = (size_t)b.smem_bytes > used ? (size_t)b.smem_bytes - used : 0;
+    return jacobi_truncate_mixed_qr(W, R, N, Wff, b.smem + used, spare, epsrel, sh.norm, sh.perm,
+                                    &sh.jsh, Wout);
+  }
   if (MIXED) {
     kk = jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh);
   } else {
@@ -219,8 +230,9 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     }
     const bool trans = n > m;
     zc* W;
-    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, b, sh, &W)
-                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, b, sh, &W);
+    bool flip;
+    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, b, sh, &W, &flip)
+                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, b, sh, &W, &flip);
     {
       const double R = trans ? n : m, N = trans ? m : n;
       flops += 8.0 * m * n * ccd + 4.0 * (6.0 * R * N * N + 20.0 * N * N * N);
@@ -233,7 +245,8 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       __syncthreads();
       break;
     }
-    if (!trans) {
+    // W = theta V (U S) or W = theta^H U (V S), by orientation and driver
+    if (!(flip ? !trans : trans)) {
       // U = W[:, perm] / s  -> site (cxd, D, kk);  carry = U^H theta
       for (int idx = tid; idx < m * kk; idx += nt) {
         const int row = idx / kk, j = idx - row * kk;
@@ -280,8 +293,9 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       const int m = D * r, n = l;
       const bool trans = n > m;
       zc* W;
-      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, b, sh, &W)
-                           : split<MIXED>(A, m, false, m, n, I.epsrel, b, sh, &W);
+      bool flip;
+      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, b, sh, &W, &flip)
+                           : split<MIXED>(A, m, false, m, n, I.epsrel, b, sh, &W, &flip);
       {
         const double R = trans ? n : m, N = trans ? m : n;
         flops += 4.0 * (6.0 * R * N * N + 20.0 * N * N * N) + 8.0 * DIMS(k - 1).x * D * (double)kk * n;
@@ -294,7 +308,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
         __syncthreads();
         break;
       }
-      if (!trans) {
+      if (!(flip ? !trans : trans)) {
         for (int idx = tid; idx < kk * n; idx += nt) {
           const int j = idx / n, col = idx - j * n;
           const int pj = sh.perm[j];
