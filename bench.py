@@ -296,7 +296,8 @@ def run_surrogate(args):
             "config": {"workload": f"MLP 5->{sizes[1]}x{len(sizes) - 2} GELU->{sizes[-1]}; "
                                    f"{args.sur_train} train / {args.sur_val} calibration / "
                                    f"{args.sur_test} held-out TEMPO trajectories, {ns} steps dt 0.05, "
-                                   f"dkmax {dk}, epsrel 1e-6; H = Omega/2 sx + eps/2 sz",
+                                   f"dkmax {dk}, epsrel 1e-6; H = Omega/2 sx + eps/2 sz; the network learns the "
+                                   f"bath's correction to the closed-system precession",
                        "error_bins": f"{args.sur_bins}x{args.sur_bins} (alpha x T)",
                        "l2": "not flushed: inference inputs and weights are the workload's resident state"},
             "inference": {"points_per_s": npts / (ms / 1e3), "points": npts, "ms": ms},
@@ -318,6 +319,125 @@ def run_surrogate(args):
     print(json.dumps(line))
 
 
+def _pt_worker(args):
+    """CPU oracle PT-TEMPO build of one instance (seconds)."""
+    inst = args
+    from oracle import tempo_oracle as to
+    infl = inst["influences"]
+    t0 = time.perf_counter()
+    to.pt_tempo_build(2, lambda dk: infl[dk] if 0 <= dk < len(infl) else None,
+                      inst["num_steps"], inst["dkmax"], inst["epsrel"])
+    return time.perf_counter() - t0
+
+
+def run_pt(args):
+    """PT-TEMPO workload: a batch of process tensors of the spin-boson model
+    (omega_c 5, T 1, dt 0.02, sigma_z/2 coupling) at alpha ~ 0.1 U[0.8, 1],
+    dkmax 20, 100 steps, epsrel 1e-6 (bonds up to ~25; the alpha 0.3,
+    epsrel 1e-7 model reaches bond 168 already at dkmax 20, beyond one CTA
+    per split), built in both precision forms; then the process-tensor sweep
+    (compute_dynamics) for 8 and for 1024 Hamiltonians a sx + b sz with
+    (a, b) ~ U[-2, 2]^2 on one process tensor.  One JSON line; ``value`` =
+    mixed-form process-tensor builds per second."""
+    import numpy as np
+    import torch
+    from oqupy_gb300 import bath
+    from oqupy_gb300.pt import PtBatch
+    n, steps, dk = args.pt_instances, args.pt_steps, args.pt_dkmax
+    rng = np.random.default_rng(20261204)
+    sz = np.diag([1.0, -1.0]).astype(complex)
+    sx = np.array([[0, 1], [1, 0]], dtype=complex)
+    insts = []
+    for _ in range(n):
+        a = 0.1 * rng.uniform(0.8, 1.0)
+        infl, _u = bath.influences(a, 1.0, 5.0, "exponential", 1.0, 0.02, dk, 0.5 * sz)
+        insts.append(dict(hs_dim=2, num_steps=steps, dkmax=dk, epsrel=1e-6,
+                          influences=infl[:min(steps, dk + 1)]))
+    res = {}
+    clocks = ClockSampler()
+    clocks.start()
+    for prec in ("mixed", "complex128"):
+        b = PtBatch(insts, precision=prec, chi_cap=args.pt_chi_cap)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.advance(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        b.check_status()
+        ms = e0.elapsed_time(e1)
+        infos = [b.info(i) for i in range(n)]
+        res[prec] = {"ms": ms, "builds_per_s": n / (ms / 1e3),
+                     "max_bond": max(int(x["max_bond"]) for x in infos),
+                     "splits": int(sum(x["splits"] for x in infos))}
+        if prec == "mixed":
+            bm = b
+        else:
+            bc = b
+    # sweep: 8 and 1024 Hamiltonians on process tensor 0
+    sweeps = {}
+    dims = bc.bond_dimensions(0)
+    for nh in (8, 1024):
+        ab = rng.uniform(-2, 2, size=(nh, 2))
+        props = [bath.half_step_propagators(a * sx + c * sz, 0.02) for a, c in ab]
+        p1 = np.array([p[0] for p in props]); p2 = np.array([p[1] for p in props])
+        rho0 = np.tile(np.array([1, 0, 0, 0], dtype=complex), (nh, 1))
+        bm.dynamics(0, p1, p2, rho0)                  # warm-up (graph build)
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            out_m = bm.dynamics(0, p1, p2, rho0)
+        dt_s = (time.perf_counter() - t0) / reps
+        out_c = bc.dynamics(0, p1, p2, rho0)
+        td = trace_distance_max(out_m, out_c).max()
+        chi = dims.astype(float)
+        pt_bytes = float(np.sum(16.0 * chi[:-1] * chi[1:] * 4))
+        st_bytes = float(np.sum(16.0 * nh * (chi[:-1] + chi[1:]) * 4))
+        flops = float(np.sum(8.0 * nh * chi[:-1] * chi[1:] * 4))
+        sweeps[str(nh)] = {"seconds_per_sweep": dt_s, "steps": steps,
+                           "us_per_step": dt_s / steps * 1e6,
+                           "effective_GBps": (pt_bytes + st_bytes) / dt_s / 1e9,
+                           "fp64_GFLOPs": flops / dt_s / 1e9,
+                           "mixed_vs_complex128_trace_distance": float(td)}
+    clk = clocks.stop()
+    cpu = None
+    if args.cpu_sample > 0:
+        import multiprocessing as mp
+        procs = os.cpu_count() or 1
+        sample = insts[: min(args.cpu_sample, n)]
+        os.environ["OPENBLAS_NUM_THREADS"] = "1"
+        with mp.get_context("spawn").Pool(min(procs, len(sample))) as pool:
+            per = pool.map(_pt_worker, sample)
+        cpu = {"value": min(procs, len(sample)) / float(np.mean(per)), "unit": "process-tensor builds/s",
+               "cores": min(procs, len(sample)), "kind": "port",
+               "sample": f"{len(sample)} builds, numpy oracle, one process per core"}
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    s1024 = sweeps["1024"]
+    from oqupy_gb300 import _native
+    fp64_peak = _native.fma_peak_tflops(0)
+    line = {"metric": "PT-TEMPO process-tensor builds/s (mixed form) and process-tensor sweep",
+            "value": res["mixed"]["builds_per_s"], "unit": "process-tensor builds/s", "n_gpus": 1,
+            "steps": steps, "warmup": 0, "ms_per_step": res["mixed"]["ms"] / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 (Jacobi in double-float)", "data": "synthetic",
+            "config": {"workload": f"{n} process tensors, spin-boson alpha~0.1*U[0.8,1], wc 5, T 1, dt 0.02, "
+                                   f"dkmax {dk}, {steps} steps, epsrel 1e-6",
+                       "chi_cap": args.pt_chi_cap},
+            "build": res, "mixed_speedup_vs_complex128": res["complex128"]["ms"] / res["mixed"]["ms"],
+            "sweep": sweeps,
+            # the sweep re-reads each PT tensor from L2 for every Hamiltonian: HBM traffic is
+            # the tensor once per step, so the bound is the FP64 pipe (complex128 sweep)
+            "roofline": {"bound": "fp64-pipe", "achieved": s1024["fp64_GFLOPs"] / 1e3,
+                         "peak": fp64_peak, "unit": "TFLOP/s", "frac": s1024["fp64_GFLOPs"] / 1e3 / fp64_peak,
+                         "traffic": None, "hbm_effective_GBps": s1024["effective_GBps"],
+                         "hbm_peak_GBps": peaks["hbm_gbs"],
+                         "kernel": "dyn_step_kernel (1024 Hamiltonians), wall time of the whole sweep call",
+                         "peak_source": "measured DFMA throughput (otb_measure_fma_peak)"},
+            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": steps * 2}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,13 +448,17 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--no-complex128", action="store_true")
     ap.add_argument("--chi-cap", type=int, default=64)
-    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate"])
+    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt"])
+    ap.add_argument("--pt-instances", type=int, default=304)
+    ap.add_argument("--pt-steps", type=int, default=100)
+    ap.add_argument("--pt-dkmax", type=int, default=20)
+    ap.add_argument("--pt-chi-cap", type=int, default=64)
     ap.add_argument("--sur-train", type=int, default=20000)
     ap.add_argument("--sur-val", type=int, default=2000)
     ap.add_argument("--sur-test", type=int, default=2000)
     ap.add_argument("--sur-steps", type=int, default=500)
     ap.add_argument("--sur-dkmax", type=int, default=8)
-    ap.add_argument("--sur-epochs", type=int, default=150)
+    ap.add_argument("--sur-epochs", type=int, default=300)
     ap.add_argument("--sur-bins", type=int, default=4)
     ap.add_argument("--sur-points", type=int, default=100000)
     args = ap.parse_args()
@@ -343,6 +467,15 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     seed = 20261203 + rank
+    if args.workload == "pt":
+        if rank != 0:
+            return
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the PT workload's CPU oracle is "
+                              "reported as cpu_baseline in the gb300 line"}))
+            return
+        run_pt(args)
+        return
     if args.workload == "surrogate":
         if rank != 0:
             return

@@ -187,6 +187,25 @@ def bloch(states: np.ndarray) -> np.ndarray:
     return np.stack([2 * r01.real, -2 * r01.imag, (states[..., 0] - states[..., 3]).real], axis=-1)
 
 
+def free_bloch(params: np.ndarray, nsteps: int, dt: float = 0.05) -> np.ndarray:
+    """Bloch trajectories [N, 3, nsteps] (steps 1..nsteps) of the system
+    without the bath: precession of (0, 0, 1) about (Omega, 0, eps) at
+    angular frequency sqrt(Omega^2 + eps^2) (Rodrigues' rotation)."""
+    p = np.asarray(params)
+    om, ep = p[:, 3], p[:, 4]
+    w = np.sqrt(om ** 2 + ep ** 2)
+    n = np.stack([om / w, np.zeros_like(om), ep / w], axis=1)          # axis
+    t = dt * np.arange(1, nsteps + 1)
+    th = w[:, None] * t[None, :]                                         # [N, T]
+    v = np.array([0.0, 0.0, 1.0])
+    ndv = n @ v                                                          # [N]
+    cross = np.cross(n, v)                                               # [N, 3]
+    out = (v[None, :, None] * np.cos(th)[:, None, :]
+           + cross[:, :, None] * np.sin(th)[:, None, :]
+           + (n * ndv[:, None])[:, :, None] * (1.0 - np.cos(th))[:, None, :])
+    return out
+
+
 def tempo_bloch(params: np.ndarray, nsteps: int, dt: float = 0.05, dkmax: int = 8,
                 epsrel: float = 1e-6, precision: str = "mixed", chi_cap: int = 64,
                 chunk: int = 4096) -> Tuple[np.ndarray, float]:
@@ -218,9 +237,11 @@ class Surrogate:
 
     def __init__(self, nsteps: int = 500, hidden: Sequence[int] = (512, 512, 512, 512),
                  dt: float = 0.05, dkmax: int = 8, epsrel: float = 1e-6, seed: int = 0,
-                 bins: int = 4, chi_cap: int = 64):
+                 bins: int = 4, chi_cap: int = 64, residual: bool = True):
         self.nsteps, self.dt, self.dkmax, self.epsrel = nsteps, dt, dkmax, epsrel
         self.chi_cap = chi_cap
+        # learn the bath's correction to the closed-system precession
+        self.residual = residual
         self.net = Mlp([5] + list(hidden) + [3 * nsteps], seed=seed)
         self.bins = bins
         self.err_map = None
@@ -236,8 +257,10 @@ class Surrogate:
             lr_final: float = 5e-5, weight_decay: float = 0.0, seed: int = 0) -> List[float]:
         torch = self.net.torch
         X = self._x(params)
-        T = torch.tensor(np.asarray(traj).reshape(len(params), -1), dtype=torch.float32,
-                         device=self.net.dev)
+        tgt = np.asarray(traj)
+        if self.residual:
+            tgt = tgt - free_bloch(params, self.nsteps, self.dt)
+        T = torch.tensor(tgt.reshape(len(params), -1), dtype=torch.float32, device=self.net.dev)
         n = X.shape[0]
         rng = np.random.default_rng(seed)
         losses = []
@@ -259,7 +282,10 @@ class Surrogate:
 
     def predict(self, params) -> np.ndarray:
         Y = self.net.forward(self._x(params))
-        return Y.cpu().numpy().reshape(len(params), 3, self.nsteps)
+        out = Y.cpu().numpy().reshape(len(params), 3, self.nsteps).astype(np.float64)
+        if self.residual:
+            out += free_bloch(params, self.nsteps, self.dt)
+        return out
 
     def _bin(self, params):
         p = np.asarray(params)
