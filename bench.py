@@ -30,6 +30,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 NSTEPS_TRAJ = 500
+DRAM_BYTES_PER_INSTANCE_STEP31 = (14.974464e6 + 0.60544e6) / 64
 METRIC = "spin-boson trajectories/sec on 1 GB300, mixed vs complex128, at 1e-6 trace dist"
 
 
@@ -586,12 +587,13 @@ def main():
         ach_c = fl_c / (t_c / 1e3) / 1e12
         roofline["complex128"] = {"bound": "fp64-pipe", "achieved": ach_c, "peak": peak_fp64,
                                   "frac": ach_c / peak_fp64}
-    prof = os.path.join(ROOT, "profiles", "tempo_kernel_traffic.json")
-    if os.path.exists(prof):
-        try:
-            roofline["traffic"] = json.load(open(prof)).get("dram_bytes_per_launch")
-        except Exception:
-            pass
+    # DRAM bytes per launch: ncu capture of the mixed kernel at step 31 for the
+    # first 64 instances of this batch (dram__bytes_read.sum + write = 15.58 MB),
+    # scaled by the instance count (every instance reads and writes only its
+    # own site ring, influences and states)
+    roofline["traffic"] = DRAM_BYTES_PER_INSTANCE_STEP31 * args.instances
+    roofline["traffic_source"] = ("ncu, step 31, 64 instances, scaled by instances "
+                                  "(profiles/tempo_kernel_mixed_step31.md)")
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
