@@ -67,7 +67,7 @@ def _oracle_worker(args):
     from oracle import tempo_oracle as to
     infl = inst["influences"]
     p1, p2 = inst["prop1"], inst["prop2"]
-    D = 4
+    D = int(np.asarray(inst["rho0"]).size)
     # negative dk asks for the add_correlation_time influence: none here
     o = to.TempoOracle(inst["rho0"].reshape(-1), lambda dk: infl[dk] if dk >= 0 else None,
                        inst["unitary"], lambda s: (p1, p2), np.ones(D),
@@ -439,6 +439,75 @@ def run_pt(args):
     print(json.dumps(line))
 
 
+def make_qutrit_instances(n, seed):
+    """Batched qutrit configuration: d = 3, super-ohmic J = 2 alpha w^3 / wc^2
+    exp(-w / wc) (zeta = 3), alpha ~ U[0.05, 0.2], wc = 3, T ~ U[0, 2],
+    H = seeded GUE 3x3 scaled to spectral norm 1, coupling diag(1, 0, -1),
+    dt 0.05, dkmax 100, epsrel 1e-7, rho0 = |0><0|, 300-step trajectories."""
+    import numpy as np
+    from oqupy_gb300 import bath
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a = rng.uniform(0.05, 0.2)
+        T = rng.uniform(0.0, 2.0)
+        g = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+        h = 0.5 * (g + g.conj().T)
+        h /= np.linalg.norm(h, 2)
+        infl, U = bath.influences(a, 3.0, 3.0, "exponential", T, 0.05, 100, np.diag([1.0, 0.0, -1.0]))
+        p1, p2 = bath.half_step_propagators(h, 0.05)
+        out.append(dict(hs_dim=3, dkmax=100, epsrel=1e-7, influences=infl, prop1=p1, prop2=p2,
+                        rho0=np.diag([1.0, 0.0, 0.0]).astype(complex), unitary=U))
+    return out
+
+
+def run_qutrit(args):
+    """Batched-qutrit workload: mixed form on the GPU over a window of steps
+    (warm-up W, timed K) against the CPU oracle on the same window.  value =
+    300-step trajectories/s at the cost of the timed steps."""
+    import numpy as np
+    import torch
+    n = args.qutrit_instances
+    insts = make_qutrit_instances(n, 20261205)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler()
+    clocks.start()
+    t_ms, ms, fl, st, stats, e2e_m = run_gpu_form(torch, insts, "mixed", args.warmup, args.steps, flush,
+                                                   args.qutrit_chi_cap, args.steps)
+    clk = clocks.stop()
+    value = n * args.steps / 300 / (t_ms / 1e3)
+    e2e_s, h2d, d2h = e2e_m
+    cpu = None
+    if args.cpu_sample > 0:
+        procs = os.cpu_count() or 1
+        sample = insts[: min(args.cpu_sample, procs)]
+        rate, cpu_s, wall = cpu_oracle_rate(sample, args.warmup, args.steps, procs)
+        rate = rate * NSTEPS_TRAJ / 300          # 300-step trajectories
+        cpu = {"value": rate, "unit": "trajectories/s", "cores": procs, "kind": "port",
+               "sample": f"{len(sample)} instances x steps {args.warmup + 1}..{args.warmup + args.steps}"
+                         f" ({cpu_s:.1f} CPU-s), numpy oracle, one process per core"}
+    from oqupy_gb300 import _native
+    peak_fp32 = _native.fma_peak_tflops(1)
+    achieved = fl / (t_ms / 1e3) / 1e12
+    line = {"metric": "batched qutrit TEMPO trajectories/sec on 1 GB300 (mixed form)", "value": value,
+            "unit": "trajectories/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128 (Jacobi in double-float)", "data": "synthetic",
+            "config": {"workload": f"{n} qutrit instances (alpha U[0.05,0.2], wc 3, T U[0,2], zeta 3, GUE H, "
+                                   "dkmax 100, dt 0.05, epsrel 1e-7, 300-step trajectories)",
+                       "timed_steps": f"{args.warmup + 1}..{args.warmup + args.steps} of 300",
+                       "chi_cap": args.qutrit_chi_cap,
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+                         "frac": achieved / peak_fp32, "traffic": None,
+                         "kernel": "tempo_kernel<true>", "peak_source": "measured FFMA throughput"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": n * args.steps / 300 / e2e_s, "unit": "trajectories/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": clk, "gpu_launches": args.steps, "mixed_stats": stats}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -449,7 +518,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--no-complex128", action="store_true")
     ap.add_argument("--chi-cap", type=int, default=64)
-    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt"])
+    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit"])
+    ap.add_argument("--qutrit-instances", type=int, default=128)
+    ap.add_argument("--qutrit-chi-cap", type=int, default=96)
     ap.add_argument("--pt-instances", type=int, default=304)
     ap.add_argument("--pt-steps", type=int, default=100)
     ap.add_argument("--pt-dkmax", type=int, default=20)
@@ -468,6 +539,15 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     seed = 20261203 + rank
+    if args.workload == "qutrit":
+        if rank != 0:
+            return
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the qutrit workload's CPU oracle is "
+                              "reported as cpu_baseline in the gb300 line"}))
+            return
+        run_qutrit(args)
+        return
     if args.workload == "pt":
         if rank != 0:
             return

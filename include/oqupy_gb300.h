@@ -263,6 +263,13 @@ otb_status otb_mlp_adamw(float* w, const float* g, float* m, float* v, void* w_b
                          int64_t n, float lr, float beta1, float beta2, float eps,
                          float weight_decay, int32_t step, void* stream);
 
+/* Surrogate output baseline (no reference counterpart): adds to y[B][3][nsteps]
+ * the Bloch vector of the bath-free system H = Omega/2 sx + eps/2 sz started
+ * in (0, 0, 1) at times dt, 2 dt, ..., nsteps dt; omega_eps[B][2] holds
+ * (Omega, eps) per point.  Device pointers. */
+otb_status otb_mlp_bloch_free_add(float* y, const float* omega_eps, int32_t B, int32_t nsteps,
+                                  float dt, void* stream);
+
 /* Measured FMA-pipe throughput of this GPU (TFLOP/s, 2 flops per FMA):
  * precision 0 = FP64 (DFMA), 1 = FP32 (FFMA).  Used as the roofline peak of
  * the Jacobi kernels, which run on these pipes. */

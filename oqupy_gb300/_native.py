@@ -120,6 +120,7 @@ def _declare(lib):
         "otb_mlp_transpose_bf16": (i32, [P, P, i32, i32, P]),
         "otb_mlp_f32_to_bf16": (i32, [P, P, ctypes.c_int64, P]),
         "otb_mlp_colsum": (i32, [P, P, i32, i32, P]),
+        "otb_mlp_bloch_free_add": (i32, [P, P, i32, i32, ctypes.c_float, P]),
         "otb_mlp_mse_grad": (i32, [P, P, P, P, ctypes.c_int64, P, P]),
         "otb_mlp_adamw": (i32, [P, P, P, P, P, ctypes.c_int64, ctypes.c_float,
                                 ctypes.c_float, ctypes.c_float, ctypes.c_float,
@@ -146,7 +147,7 @@ def exported_symbols():
         "otb_pt_advance", "otb_pt_get_info", "otb_pt_bond_dims",
         "otb_pt_get_tensor", "otb_pt_get_cap", "otb_dyn_run", "otb_mlp_gemm",
         "otb_mlp_transpose_bf16", "otb_mlp_f32_to_bf16", "otb_mlp_colsum",
-        "otb_mlp_mse_grad", "otb_mlp_adamw",
+        "otb_mlp_mse_grad", "otb_mlp_adamw", "otb_mlp_bloch_free_add",
         "otb_measure_fma_peak", "otb_last_error", "otb_version"]
 
 

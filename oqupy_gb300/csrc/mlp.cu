@@ -255,6 +255,27 @@ __global__ void adamw_kernel(float* __restrict__ w, const float* __restrict__ g,
   }
 }
 
+// y[b][c * nsteps + t] += Bloch component c at time (t + 1) dt of the system
+// without the bath: precession of (0, 0, 1) about (Omega, 0, eps) at angular
+// frequency w = sqrt(Omega^2 + eps^2) (Rodrigues' rotation).
+__global__ void bloch_free_add_kernel(float* __restrict__ y, const float* __restrict__ oe, int B, int nsteps,
+                                      float dt) {
+  const long long total = (long long)B * nsteps;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / nsteps), t = (int)(i - (long long)b * nsteps);
+    const float om = oe[2 * b], ep = oe[2 * b + 1];
+    const float w = sqrtf(om * om + ep * ep);
+    const float nx = w > 0.f ? om / w : 0.f, nz = w > 0.f ? ep / w : 1.f;
+    float s, c;
+    sincosf(w * dt * (float)(t + 1), &s, &c);
+    float* row = y + (size_t)b * 3 * nsteps;
+    row[t] += nx * nz * (1.f - c);
+    row[nsteps + t] += -nx * s;
+    row[2 * nsteps + t] += c + nz * nz * (1.f - c);
+  }
+}
+
 }  // namespace otb
 
 using namespace otb;
@@ -314,5 +335,14 @@ extern "C" otb_status otb_mlp_adamw(float* w, const float* g, float* m, float* v
   adamw_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(w, g, m, v, (__nv_bfloat16*)w_bf16, n, lr, beta1, beta2, eps,
                                                        weight_decay, c1, c2);
   if (!check_cuda(cudaGetLastError(), "adamw")) return OTB_ERR_CUDA;
+  return OTB_OK;
+}
+
+extern "C" otb_status otb_mlp_bloch_free_add(float* y, const float* omega_eps, int32_t B, int32_t nsteps, float dt,
+                                            void* stream) {
+  if (!y || !omega_eps || B <= 0 || nsteps <= 0 || !(dt > 0.f))
+    return set_error(OTB_ERR_INVALID_ARG, "bad bloch arguments");
+  bloch_free_add_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(y, omega_eps, B, nsteps, dt);
+  if (!check_cuda(cudaGetLastError(), "bloch free add")) return OTB_ERR_CUDA;
   return OTB_OK;
 }

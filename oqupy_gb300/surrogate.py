@@ -281,11 +281,15 @@ class Surrogate:
         return losses
 
     def predict(self, params) -> np.ndarray:
-        Y = self.net.forward(self._x(params))
-        out = Y.cpu().numpy().reshape(len(params), 3, self.nsteps).astype(np.float64)
+        """Bloch trajectories [N, 3, nsteps] (float32) for ``params``."""
+        torch = self.net.torch
+        p = np.asarray(params)
+        Y = self.net.forward(self._x(p))
         if self.residual:
-            out += free_bloch(params, self.nsteps, self.dt)
-        return out
+            oe = torch.tensor(p[:, 3:5], dtype=torch.float32, device=self.net.dev)
+            nat.check(nat.lib().otb_mlp_bloch_free_add(Y.data_ptr(), oe.data_ptr(), len(p), self.nsteps,
+                                                       float(self.dt), None))
+        return Y.cpu().numpy().reshape(len(p), 3, self.nsteps)
 
     def _bin(self, params):
         p = np.asarray(params)
@@ -313,7 +317,7 @@ class Surrogate:
         Returns (trajectories, fallback mask, timings)."""
         p = np.asarray(params)
         t0 = time.perf_counter()
-        out = self.predict(p)
+        out = self.predict(p).astype(np.float64)
         t_sur = time.perf_counter() - t0
         trusted = self.in_box(p) & (self.err_map[self._bin(p)] <= budget)
         fb = ~trusted

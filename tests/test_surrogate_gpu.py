@@ -90,3 +90,18 @@ def test_screening_falls_back_outside_budget_and_box():
     # calibrated on held-out points of the same regions: allow a margin
     assert np.quantile(trusted_err, 0.9) <= 2.0 * budget
     assert tim["points_per_s"] > 0
+
+
+def test_device_baseline_matches_host_precession():
+    """otb_mlp_bloch_free_add against the float64 host baseline (float32
+    phases up to ~55 rad: tolerance 2e-5)."""
+    import torch
+    from oqupy_gb300 import _native as nat
+    from oqupy_gb300.surrogate import free_bloch, sample_params
+    P = sample_params(300, 21)
+    nsteps, dt = 500, 0.05
+    y = torch.zeros((len(P), 3 * nsteps), dtype=torch.float32, device="cuda")
+    oe = torch.tensor(P[:, 3:5], dtype=torch.float32, device="cuda")
+    nat.check(nat.lib().otb_mlp_bloch_free_add(y.data_ptr(), oe.data_ptr(), len(P), nsteps, dt, None))
+    got = y.cpu().numpy().reshape(len(P), 3, nsteps)
+    np.testing.assert_allclose(got, free_bloch(P, nsteps, dt), atol=2e-5)
