@@ -173,13 +173,13 @@ def trace_distance_max(a, b):
 
 
 def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_steps=0):
-    """Warm-up, ``steps`` device-timed steps, then ``e2e_steps`` steps through
-    the per-step plugin path (propagators host->device, advance, states
-    device->host), wall-clock timed."""
+    """Warm-up, ``steps`` device-timed steps; then, on a fresh batch advanced
+    through the same warm-up, ``e2e_steps`` steps of the same window through
+    the plugin path (all propagators host->device in one call, one launch,
+    the new states device->host), wall-clock timed."""
     import numpy as np
     from oqupy_gb300 import TempoBatch
-    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap,
-                   out_cap=warm + steps + e2e_steps + 1)
+    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + steps + 1)
     stream = torch.cuda.current_stream()
     for _ in range(warm):
         b.advance(1, stream.cuda_stream)
@@ -198,25 +198,33 @@ def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_st
     b.check_status()
     infos = [b.info(i) for i in range(b.n)]
     flops = sum(x["flops_alg"] for x in infos) - f0
-    e2e = None
-    if e2e_steps:
-        h2d = d2h = 0
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(e2e_steps):
-            for i, inst in enumerate(insts):
-                b.set_propagators(i, inst["prop1"], inst["prop2"], inst["unitary"])
-                h2d += 2 * inst["prop1"].nbytes
-            b.advance(1, stream.cuda_stream)
-            st = b.states(warm + steps + k + 1, 1)
-            d2h += st.nbytes
-        e2e = (time.perf_counter() - t0, h2d // e2e_steps, d2h // e2e_steps)
     states = b.states(0, warm + steps + 1)
     nsplit = max(1, sum(x["splits"] for x in infos))
     stats = {"max_bond": max(x["max_bond"] for x in infos), "splits": nsplit,
              "sweeps64_per_split": sum(x["sweeps64"] for x in infos) / nsplit,
              "sweepsff_per_split": sum(x["sweeps32"] for x in infos) / nsplit}
     b.close()
+    e2e = None
+    if e2e_steps:
+        b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + e2e_steps + 1)
+        for _ in range(warm):
+            b.advance(1, stream.cuda_stream)
+        torch.cuda.synchronize()
+        p1s = [i["prop1"] for i in insts]
+        p2s = [i["prop2"] for i in insts]
+        us = [i.get("unitary") for i in insts]
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            flush.zero_()
+            b.set_all_propagators(p1s, p2s, us, stream.cuda_stream)
+            h2d += 2 * sum(np.asarray(p).nbytes for p in p1s)
+            b.advance(1, stream.cuda_stream)
+            st = b.states(warm + k + 1, 1)
+            d2h += st.nbytes
+        e2e = (time.perf_counter() - t0, h2d // e2e_steps, d2h // e2e_steps)
+        b.check_status()
+        b.close()
     return sum(ms), ms, flops, states, stats, e2e
 
 
@@ -642,9 +650,10 @@ def main():
     e2e_s, h2d, d2h = e2e_m
     e2e = {"value": world * args.instances * args.steps / NSTEPS_TRAJ / e2e_s,
            "unit": "trajectories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "note": (f"steps {args.warmup + args.steps + 1}..{args.warmup + 2 * args.steps} through "
-                    "the per-step plugin path: propagators host->device for every instance, "
-                    "one launch, new states device->host; wall clock")}
+           "note": (f"steps {args.warmup + 1}..{args.warmup + args.steps} (the timed window, on a "
+                    "second batch advanced through the same warm-up) through the plugin path: "
+                    "all propagators host->device in one call, one launch, the new states "
+                    "device->host; wall clock")}
     # cost-model projection to whole 500-step trajectories (work per step taken
     # proportional to the memory window; bond-dimension growth not modelled)
     timed_sites = window_sites(insts, args.warmup + 1, args.warmup + args.steps) / args.steps

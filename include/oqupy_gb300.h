@@ -115,6 +115,15 @@ otb_status otb_tempo_set_influence(otb_tempo* h, int32_t inst, int32_t dk,
 /* Propagators for the next step (time-dependent systems, tempo.py:400-435). */
 otb_status otb_tempo_set_propagators(otb_tempo* h, int32_t inst,
                                      const double* prop1, const double* prop2);
+/* Propagators of every instance for the next step in one call: p1, p2 hold
+ * the instances' D x D matrices packed in instance order (eigenbasis-folded
+ * like otb_tempo_set_propagators).  Ordered on `stream` before the next
+ * otb_tempo_advance on that stream; from page-locked host memory the copy is
+ * asynchronous and the buffers must stay valid until it completes.  The
+ * batched form of the per-step propagators(step) call of
+ * TempoBackend.compute_step (tempo_backend.py:619-626). */
+otb_status otb_tempo_set_all_propagators(otb_tempo* h, const double* prop1,
+                                         const double* prop2, void* stream);
 /* Influence replacing the oldest window site in the next step only
  * (add_correlation_time, tempo_backend.py:503-517). */
 otb_status otb_tempo_set_first_influence(otb_tempo* h, int32_t inst,

@@ -435,6 +435,42 @@ extern "C" otb_status otb_tempo_set_propagators(otb_tempo* h, int32_t inst, cons
   return OTB_OK;
 }
 
+extern "C" otb_status otb_tempo_set_all_propagators(otb_tempo* h, const double* p1, const double* p2,
+                                                    void* stream) {
+  if (!h) return set_error(OTB_ERR_INVALID_ARG, "null handle");
+  if (!p1 || !p2) return set_error(OTB_ERR_INVALID_ARG, "null propagator");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)h->inst.size();
+  bool uniform = true;
+  for (int i = 1; i < n && uniform; ++i)
+    uniform = h->inst[i].D == h->inst[0].D &&
+              h->inst[i].prop_base - h->inst[i - 1].prop_base ==
+                  (n > 1 ? h->inst[1].prop_base - h->inst[0].prop_base : 0);
+  if (uniform && n > 1) {
+    // one strided copy per propagator: instance i's P1 / P2 sit at a fixed pitch
+    const int D = h->inst[0].D;
+    const size_t w = (size_t)D * D * 2 * sizeof(double);
+    const size_t pitch = (size_t)(h->inst[1].prop_base - h->inst[0].prop_base) * 2 * sizeof(double);
+    double* base = (double*)h->d_props.p + 2 * h->inst[0].prop_base;
+    if (!check_cuda(cudaMemcpy2DAsync(base, pitch, p1, w, w, n, cudaMemcpyHostToDevice, s), "set all prop1") ||
+        !check_cuda(cudaMemcpy2DAsync(base + 2 * D * D, pitch, p2, w, w, n, cudaMemcpyHostToDevice, s),
+                    "set all prop2"))
+      return OTB_ERR_CUDA;
+    return OTB_OK;
+  }
+  size_t off = 0;
+  for (int i = 0; i < n; ++i) {
+    const InstDev& I = h->inst[i];
+    const size_t b = (size_t)I.D * I.D * 2 * sizeof(double);
+    double* base = (double*)h->d_props.p + 2 * I.prop_base;
+    if (!check_cuda(cudaMemcpyAsync(base, p1 + off, b, cudaMemcpyHostToDevice, s), "set prop1") ||
+        !check_cuda(cudaMemcpyAsync(base + 2 * I.D * I.D, p2 + off, b, cudaMemcpyHostToDevice, s), "set prop2"))
+      return OTB_ERR_CUDA;
+    off += (size_t)I.D * I.D * 2;
+  }
+  return OTB_OK;
+}
+
 extern "C" otb_status otb_tempo_set_first_influence(otb_tempo* h, int32_t inst, const double* mat) {
   otb_status st = check_inst(h, inst);
   if (st) return st;

@@ -171,6 +171,24 @@ class TempoBatch:
         a, b = nat.cplx(a), nat.cplx(b)
         nat.check(nat.lib().otb_tempo_set_propagators(self._h, int(i), nat.dptr(a), nat.dptr(b)))
 
+    def set_all_propagators(self, p1s, p2s, unitaries=None, stream: Optional[int] = None):
+        """Propagators of every instance for the next step in one call.
+        ``p1s``, ``p2s``: ``[n, D, D]`` (uniform D) or sequences; optional
+        coupling eigenbases ``unitaries`` are folded in as for
+        ``set_propagators``."""
+        if unitaries is None:
+            unitaries = [None] * self.n
+        if len(set(self.D)) == 1 and all(u is None for u in unitaries):
+            a = nat.cplx(np.asarray(p1s).reshape(self.n, self.D[0], self.D[0]))
+            b = nat.cplx(np.asarray(p2s).reshape(self.n, self.D[0], self.D[0]))
+        else:
+            folded = [fold_propagators(x, y, u) for x, y, u in zip(p1s, p2s, unitaries)]
+            a = nat.cplx(np.concatenate([np.asarray(f[0]).reshape(-1) for f in folded]))
+            b = nat.cplx(np.concatenate([np.asarray(f[1]).reshape(-1) for f in folded]))
+        self._staged = (a, b)          # alive until the (possibly asynchronous) copy ran
+        nat.check(nat.lib().otb_tempo_set_all_propagators(self._h, nat.dptr(a), nat.dptr(b),
+                                                          ctypes.c_void_p(stream or 0)))
+
     def set_first_influence(self, i: int, mat=None):
         if mat is None:
             nat.check(nat.lib().otb_tempo_set_first_influence(self._h, int(i), None))

@@ -89,3 +89,31 @@ def test_gpu_tempo_mixed_precision_matches_reference(name):
     print(f"{name}: mixed-precision max trace distance {max(errs):.2e}")
     bad = gc.parity_violations(errs, g["tempo_envelope"], gc.MIXED_ABS)
     assert not bad, bad[:5]
+
+
+def test_set_all_propagators_equals_per_instance_setter():
+    """One batched upload of every instance's propagators (strided copy)
+    gives bit-identical states to per-instance uploads, with the
+    eigenbasis folding applied, for time-dependent propagators."""
+    from oqupy_gb300 import TempoBatch
+    names = ["config1_spin_boson", "nondiag_coupling", "batched_like_hot"]
+    gs = [gc.load(n) for n in names]
+    insts = [dict(hs_dim=g["d"], dkmax=g["dkmax"], epsrel=g["epsrel"],
+                  influences=g["tempo_infl"][: g["dkmax"] + 1], prop1=g["prop1"][0],
+                  prop2=g["prop2"][0], rho0=g["rho0"], unitary=g["unitary"]) for g in gs]
+    nsteps = 8
+    a = TempoBatch(insts, out_cap=nsteps + 1)
+    b = TempoBatch(insts, out_cap=nsteps + 1)
+    rng = np.random.default_rng(4)
+    for step in range(nsteps):
+        # a different (non-unitary but well-scaled) propagator pair every step
+        p1s = [i["prop1"] @ (np.eye(4) + 0.01 * rng.normal(size=(4, 4))) for i in insts]
+        p2s = [i["prop2"] @ (np.eye(4) + 0.01 * rng.normal(size=(4, 4))) for i in insts]
+        for k, inst in enumerate(insts):
+            a.set_propagators(k, p1s[k], p2s[k], inst["unitary"])
+        b.set_all_propagators(p1s, p2s, [i["unitary"] for i in insts])
+        a.advance(1)
+        b.advance(1)
+    a.check_status()
+    b.check_status()
+    np.testing.assert_array_equal(a.states(0, nsteps + 1), b.states(0, nsteps + 1))
