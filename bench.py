@@ -516,6 +516,51 @@ def run_qutrit(args):
     print(json.dumps(line))
 
 
+def run_full_trajectories(args, insts, workload):
+    """Mixed form over whole 500-step trajectories of the batch: 3 warm-up
+    steps on a separate batch, then a fresh batch timed step by step (CUDA
+    events on the launching stream, L2 flushed before every step)."""
+    import numpy as np
+    import torch
+    from oqupy_gb300 import TempoBatch
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    cap = max(args.chi_cap, 96)           # bonds keep growing past the default window
+    w = TempoBatch(insts, precision="mixed", chi_cap=cap, out_cap=4)
+    for _ in range(max(3, args.warmup if args.warmup < 10 else 3)):
+        w.advance(1, stream.cuda_stream)
+    torch.cuda.synchronize()
+    w.close()
+    b = TempoBatch(insts, precision="mixed", chi_cap=cap, out_cap=NSTEPS_TRAJ + 1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(NSTEPS_TRAJ)]
+    clocks = ClockSampler()
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(NSTEPS_TRAJ):
+        flush.zero_()
+        ev[k][0].record(stream)
+        b.advance(1, stream.cuda_stream)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = np.array([a.elapsed_time(c) for a, c in ev])
+    b.check_status()
+    infos = [b.info(i) for i in range(b.n)]
+    b.close()
+    total = float(ms.sum()) / 1e3
+    line = {"metric": METRIC, "value": len(insts) / total, "unit": "trajectories/s", "n_gpus": 1,
+            "steps": NSTEPS_TRAJ, "warmup": 3, "ms_per_step": float(ms.mean()), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (Jacobi in double-float)",
+            "data": "synthetic",
+            "config": dict(workload, timed_steps=f"1..{NSTEPS_TRAJ} (whole trajectories)", precision="mixed"),
+            "ms_per_step_by_block": [float(ms[i:i + 50].mean()) for i in range(0, NSTEPS_TRAJ, 50)],
+            "max_bond": max(int(x["max_bond"]) for x in infos),
+            "splits": int(sum(x["splits"] for x in infos)), "clocks": clk,
+            "gpu_launches": NSTEPS_TRAJ}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -526,6 +571,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--no-complex128", action="store_true")
     ap.add_argument("--chi-cap", type=int, default=64)
+    ap.add_argument("--full-trajectories", action="store_true",
+                    help="time whole 500-step trajectories of the batch (mixed form only)")
     ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit"])
     ap.add_argument("--qutrit-instances", type=int, default=128)
     ap.add_argument("--qutrit-chi-cap", type=int, default=96)
@@ -612,6 +659,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from oqupy_gb300 import _native
     insts = make_instances(args.instances, seed)
+    if args.full_trajectories:
+        if rank == 0:
+            run_full_trajectories(args, insts, workload)
+        return
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():

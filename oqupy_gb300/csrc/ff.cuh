@@ -78,4 +78,51 @@ __device__ __forceinline__ cff cff_from(cx<double> z) {
 }
 __device__ __forceinline__ cx<double> cff_to(cff z) { return mk<double>(ff_to(z.x), ff_to(z.y)); }
 
+// Compensated complex multiply-accumulate for contractions: the running sum
+// is kept as (hi, lo) per component; every FF x FF product contributes its
+// exact leading product through an error-free two-sum into hi and all error
+// terms (product and sum errors, cross terms) into lo.  Relative accuracy
+// ~n * 2^-47 over an n-term sum, on the FP32 pipe only.
+struct ccacc {
+  float xh, xl, yh, yl;
+};
+
+__device__ __forceinline__ void ffp_acc(float ah, float al, float bh, float bl, float& sh, float& sl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  const float t = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+__device__ __forceinline__ ccacc ccacc_zero() {
+  ccacc a;
+  a.xh = a.xl = a.yh = a.yl = 0.f;
+  return a;
+}
+
+// acc += a * b
+__device__ __forceinline__ void ccacc_fma(ccacc& acc, const cff& a, const cff& b) {
+  ffp_acc(a.x.hi, a.x.lo, b.x.hi, b.x.lo, acc.xh, acc.xl);
+  ffp_acc(-a.y.hi, -a.y.lo, b.y.hi, b.y.lo, acc.xh, acc.xl);
+  ffp_acc(a.x.hi, a.x.lo, b.y.hi, b.y.lo, acc.yh, acc.yl);
+  ffp_acc(a.y.hi, a.y.lo, b.x.hi, b.x.lo, acc.yh, acc.yl);
+}
+
+// acc += conj(a) * b
+__device__ __forceinline__ void ccacc_fmaj(ccacc& acc, const cff& a, const cff& b) {
+  ffp_acc(a.x.hi, a.x.lo, b.x.hi, b.x.lo, acc.xh, acc.xl);
+  ffp_acc(a.y.hi, a.y.lo, b.y.hi, b.y.lo, acc.xh, acc.xl);
+  ffp_acc(a.x.hi, a.x.lo, b.y.hi, b.y.lo, acc.yh, acc.yl);
+  ffp_acc(-a.y.hi, -a.y.lo, b.x.hi, b.x.lo, acc.yh, acc.yl);
+}
+
+__device__ __forceinline__ cx<double> ccacc_value(const ccacc& a) {
+  return mk<double>((double)a.xh + (double)a.xl, (double)a.yh + (double)a.yl);
+}
+
 }  // namespace otb

@@ -200,6 +200,16 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     const int n = r * D;
     const zc* C = b.Cg;
     const bool last = (k == K - 1);
+    // mixed form: the contraction runs in double-float on the FP32 pipe, its
+    // operands converted once per element (carry -> Wffg, site -> Wg)
+    const bool ffc = MIXED && k > 0;
+    const cff* Cf = b.Wffg;
+    const cff* Af = reinterpret_cast<const cff*>(b.Wg);
+    if (ffc) {
+      for (int idx = tid; idx < cxd * ccd * D; idx += nt) b.Wffg[idx] = cff_from(C[idx]);
+      for (int idx = tid; idx < ccd * D * r; idx += nt) reinterpret_cast<cff*>(b.Wg)[idx] = cff_from(A[idx]);
+      __syncthreads();
+    }
     // theta into Tg: column-major (ld m) for a split, site layout for the last site
     for (int idx = tid; idx < m * n; idx += nt) {
       int row, col;
@@ -215,6 +225,11 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       zc acc = mk<double>(0, 0);
       if (k == 0) {
         acc = A[a * r + rr];
+      } else if (ffc) {
+        ccacc f = ccacc_zero();
+        for (int c = 0; c < ccd; ++c)
+          ccacc_fma(f, Cf[(long long)x * (ccd * D) + c * D + mr], Af[((long long)c * D + a) * r + rr]);
+        acc = ccacc_value(f);
       } else {
         for (int c = 0; c < ccd; ++c)
           cfma(acc, C[(long long)x * (ccd * D) + c * D + mr], A[((long long)c * D + a) * r + rr]);
@@ -246,7 +261,52 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       break;
     }
     // W = theta V (U S) or W = theta^H U (V S), by orientation and driver
-    if (!(flip ? !trans : trans)) {
+    const bool wt = flip ? !trans : trans;
+    if (MIXED && flip) {
+      // double-float products: theta -> Wg (the split's result lives in the
+      // Wff storage, so Wg is free), the kept columns of W -> Tg (theta's FP64
+      // copy is no longer read)
+      cff* Tf = reinterpret_cast<cff*>(b.Wg);
+      for (int idx = tid; idx < m * n; idx += nt) Tf[idx] = cff_from(b.Tg[idx]);
+      __syncthreads();
+      cff* Wf = reinterpret_cast<cff*>(b.Tg);
+      const int ldw = wt ? n : m;
+      for (int idx = tid; idx < kk * ldw; idx += nt) {
+        const int j = idx / ldw, q = idx - j * ldw;
+        Wf[idx] = cff_from(W[(long long)sh.perm[j] * ldw + q]);
+      }
+      __syncthreads();
+      if (!wt) {
+        // U = W[:, perm] / s -> site;  carry = U^H theta
+        for (int idx = tid; idx < m * kk; idx += nt) {
+          const int row = idx / kk, j = idx - row * kk;
+          const int pj = sh.perm[j];
+          A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
+        }
+        for (int idx = tid; idx < kk * n; idx += nt) {
+          const int j = idx / n, col = idx - j * n;
+          const cff* u = Wf + (long long)j * m;
+          const cff* th = Tf + (long long)col * m;
+          ccacc f = ccacc_zero();
+          for (int row = 0; row < m; ++row) ccacc_fmaj(f, u[row], th[row]);
+          b.Cg[idx] = cscale(ccacc_value(f), 1.0 / sh.norm[sh.perm[j]]);
+        }
+      } else {
+        // U = theta W[:, perm] / s^2 -> site;  carry = W[:, perm]^H
+        for (int idx = tid; idx < m * kk; idx += nt) {
+          const int row = idx / kk, j = idx - row * kk;
+          const double sj = sh.norm[sh.perm[j]];
+          const cff* w = Wf + (long long)j * n;
+          ccacc f = ccacc_zero();
+          for (int col = 0; col < n; ++col) ccacc_fma(f, Tf[(long long)col * m + row], w[col]);
+          A[idx] = cscale(ccacc_value(f), 1.0 / (sj * sj));
+        }
+        for (int idx = tid; idx < kk * n; idx += nt) {
+          const int j = idx / n, col = idx - j * n;
+          b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
+        }
+      }
+    } else if (!wt) {
       // U = W[:, perm] / s  -> site (cxd, D, kk);  carry = U^H theta
       for (int idx = tid; idx < m * kk; idx += nt) {
         const int row = idx / kk, j = idx - row * kk;
@@ -308,7 +368,51 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
         __syncthreads();
         break;
       }
-      if (!(flip ? !trans : trans)) {
+      const bool wt = flip ? !trans : trans;
+      if (MIXED && flip) {
+        // double-float products; the site -> Wg, the kept columns of W -> Tg
+        // (first branch) or Cg (second branch, whose Tg holds the product)
+        cff* Af = reinterpret_cast<cff*>(b.Wg);
+        for (int idx = tid; idx < m * n; idx += nt) Af[idx] = cff_from(A[idx]);
+        const int ldw = wt ? n : m;
+        cff* Wf = reinterpret_cast<cff*>(wt ? b.Cg : b.Tg);
+        for (int idx = tid; idx < kk * ldw; idx += nt) {
+          const int j = idx / ldw, q = idx - j * ldw;
+          Wf[idx] = cff_from(W[(long long)sh.perm[j] * ldw + q]);
+        }
+        __syncthreads();
+        if (!wt) {
+          for (int idx = tid; idx < kk * n; idx += nt) {
+            const int j = idx / n, col = idx - j * n;
+            const cff* u = Wf + (long long)j * m;
+            const cff* y = Af + (long long)col * m;
+            ccacc f = ccacc_zero();
+            for (int row = 0; row < m; ++row) ccacc_fmaj(f, u[row], y[row]);
+            b.Cg[idx] = cscale(ccacc_value(f), 1.0 / sh.norm[sh.perm[j]]);
+          }
+          __syncthreads();
+          for (int idx = tid; idx < m * kk; idx += nt) {
+            const int j = idx / m, row = idx - j * m;
+            const int pj = sh.perm[j];
+            A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
+          }
+        } else {
+          for (int idx = tid; idx < m * kk; idx += nt) {
+            const int j = idx / m, row = idx - j * m;
+            const double sj = sh.norm[sh.perm[j]];
+            const cff* w = Wf + (long long)j * n;
+            ccacc f = ccacc_zero();
+            for (int col = 0; col < n; ++col) ccacc_fma(f, Af[(long long)col * m + row], w[col]);
+            b.Tg[idx] = cscale(ccacc_value(f), 1.0 / (sj * sj));
+          }
+          __syncthreads();   // Wf (in Cg) is read above; the carry overwrites it
+          for (int idx = tid; idx < kk * n; idx += nt) {
+            const int j = idx / n, col = idx - j * n;
+            b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
+          }
+          for (int idx = tid; idx < m * kk; idx += nt) A[idx] = b.Tg[idx];
+        }
+      } else if (!wt) {
         for (int idx = tid; idx < kk * n; idx += nt) {
           const int j = idx / n, col = idx - j * n;
           const int pj = sh.perm[j];
@@ -346,13 +450,29 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       // absorb S V^H into site k-1: (l2, D, n) x (kk, n)^T -> (l2, D, kk)
       zc* B = SITE(k - 1);
       const int l2 = DIMS(k - 1).x;
-      for (int idx = tid; idx < l2 * D * kk; idx += nt) {
-        const int la = idx / kk, j = idx - la * kk;
-        const zc* brow = B + (long long)la * n;
-        const zc* crow = b.Cg + (long long)j * n;
-        zc acc = mk<double>(0, 0);
-        for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
-        b.Tg[idx] = acc;
+      if (MIXED) {
+        // double-float: site k-1 -> Wg, carry -> Wffg (the split's result is dead)
+        cff* Bf = reinterpret_cast<cff*>(b.Wg);
+        for (int idx = tid; idx < l2 * D * n; idx += nt) Bf[idx] = cff_from(B[idx]);
+        for (int idx = tid; idx < kk * n; idx += nt) b.Wffg[idx] = cff_from(b.Cg[idx]);
+        __syncthreads();
+        for (int idx = tid; idx < l2 * D * kk; idx += nt) {
+          const int la = idx / kk, j = idx - la * kk;
+          const cff* brow = Bf + (long long)la * n;
+          const cff* crow = b.Wffg + (long long)j * n;
+          ccacc f = ccacc_zero();
+          for (int c = 0; c < n; ++c) ccacc_fma(f, brow[c], crow[c]);
+          b.Tg[idx] = ccacc_value(f);
+        }
+      } else {
+        for (int idx = tid; idx < l2 * D * kk; idx += nt) {
+          const int la = idx / kk, j = idx - la * kk;
+          const zc* brow = B + (long long)la * n;
+          const zc* crow = b.Cg + (long long)j * n;
+          zc acc = mk<double>(0, 0);
+          for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
+          b.Tg[idx] = acc;
+        }
       }
       __syncthreads();
       for (int idx = tid; idx < l2 * D * kk; idx += nt) B[idx] = b.Tg[idx];
