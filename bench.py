@@ -228,11 +228,6 @@ def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_st
     return sum(ms), ms, flops, states, stats, e2e
 
 
-def window_sites(insts, first, last):
-    """Sum over instances and steps first..last of the memory window."""
-    return sum(min(s, i["dkmax"] + 1) for i in insts for s in range(first, last + 1))
-
-
 def run_surrogate(args):
     """Learned-surrogate workload: data from the batched TEMPO solver, GPU
     training with the tensor-core kernels, calibration, held-out screening
@@ -705,15 +700,6 @@ def main():
                     "second batch advanced through the same warm-up) through the plugin path: "
                     "all propagators host->device in one call, one launch, the new states "
                     "device->host; wall clock")}
-    # cost-model projection to whole 500-step trajectories (work per step taken
-    # proportional to the memory window; bond-dimension growth not modelled)
-    timed_sites = window_sites(insts, args.warmup + 1, args.warmup + args.steps) / args.steps
-    traj_sites = window_sites(insts, 1, NSTEPS_TRAJ) / NSTEPS_TRAJ
-    projection = {"value": value * timed_sites / traj_sites, "unit": "trajectories/s",
-                  "model": "per-step work proportional to sum of memory windows min(step, dkmax+1); "
-                           f"timed steps average {timed_sites:.0f} sites/step vs {traj_sites:.0f} over "
-                           "full trajectories; bond-dimension growth not modelled (optimistic)"}
-
     peak_fp32 = _native.fma_peak_tflops(1)
     peak_fp64 = _native.fma_peak_tflops(0)
     achieved = fl_mixed / t_mixed_s / 1e12
@@ -753,7 +739,10 @@ def main():
                                                     parallelism=f"instances x {world} GPUs"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "gpu_launches": args.steps, "mixed_stats": stats_mixed,
-                "full_trajectory_projection": projection}
+                "whole_trajectories": ("value is trajectory-equivalents at the cost of the timed "
+                                       "steps; per-step cost grows ~15x over a 500-step trajectory "
+                                       "(longer memory windows, larger bonds): whole trajectories "
+                                       "are timed by `python bench.py --full-trajectories`")}
         line.update(res)
         print(json.dumps(line))
     if world > 1:

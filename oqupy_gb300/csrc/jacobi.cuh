@@ -15,11 +15,15 @@
 // products are reduced with xor shuffles inside the group.  Column norms,
 // the descending sort, the tail sums and the rank decision are always FP64.
 //
-// Two drivers:
-//  * complex128: FP64 sweeps on the matrix until no pair rotates;
-//  * mixed: FP32 sweeps on an FP32 copy with the rotations accumulated in an
-//    FP32 V, then B = A V formed in FP64 and FP64 sweeps on B, which start
-//    from nearly orthogonal columns and converge in a few sweeps.
+// Drivers:
+//  * complex128 (jacobi_truncate_fp64): FP64 sweeps on the matrix until no
+//    pair rotates;
+//  * mixed, small splits (jacobi_truncate_mixed): the same sweeps in
+//    double-float arithmetic (ff.cuh) on the FP32 pipe, FP64 fallback sweeps
+//    if they do not settle;
+//  * mixed (jacobi_truncate_mixed_qr, >= 8 columns): rank-revealing pivoted
+//    Householder QR in double-float, then the double-float sweeps on the k
+//    rows of R (described above the function).
 #pragma once
 
 #include "common.cuh"

@@ -578,8 +578,9 @@ __global__ void __launch_bounds__(TEMPO_THREADS) tempo_kernel(TempoLaunch L) {
 }
 
 int tempo_smem_bytes(int precision) {
-  // dynamic shared memory for the working matrices: two CTAs per SM
-  // together with the static SharedStep block
+  // dynamic shared memory for the working matrices when the caller gives
+  // none (the C ABI passes its own default, 56 KiB: three CTAs per SM with
+  // the static SharedStep block)
   (void)precision;
   return 88 * 1024;
 }
