@@ -34,6 +34,25 @@ DRAM_BYTES_PER_INSTANCE_STEP31 = (14.974464e6 + 0.60544e6) / 64
 METRIC = "spin-boson trajectories/sec on 1 GB300, mixed vs complex128, at 1e-6 trace dist"
 
 
+def rank_seed(rank):
+    """Every rank draws its own batch of independent instances (weak scaling:
+    the ranks share no data and exchange nothing but the timing reduction)."""
+    return 20261203 + rank
+
+
+def max_over_ranks(seconds, world):
+    """Wall time of the whole job = the slowest rank (NCCL on GPUs, gloo on
+    the CPU)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_instances(n, seed):
     import numpy as np
     from oqupy_gb300 import bath
@@ -588,7 +607,7 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    seed = 20261203 + rank
+    seed = rank_seed(rank)
     if args.workload == "qutrit":
         if rank != 0:
             return
@@ -672,11 +691,7 @@ def main():
         torch, insts, "mixed", args.warmup, args.steps, flush, args.chi_cap, args.steps)
     clk = clocks.stop()
     barrier()
-    t_mixed_s = t_mixed / 1e3
-    if world > 1:
-        t = torch.tensor([t_mixed_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_mixed_s = float(t.item())
+    t_mixed_s = max_over_ranks(t_mixed / 1e3, world)
     value = world * args.instances * args.steps / NSTEPS_TRAJ / t_mixed_s
 
     res = {}
