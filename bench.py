@@ -137,7 +137,8 @@ class ClockSampler:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), f"oqupy_gb300_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

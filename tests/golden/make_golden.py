@@ -50,7 +50,7 @@ def cases(oqupy):
     sm = oqupy.operators.sigma("-")
     up = oqupy.operators.spin_dm("up")
     rng = np.random.default_rng(1234)
-    # BASELINE configs[0]: plain TEMPO spin-boson
+    # plain TEMPO spin-boson (alpha 0.08, wc 4, T 0, dkmax 20, 100 steps)
     yield "config1_spin_boson", dict(
         h=0.5 * 1.0 * sx, gammas=[], lops=[], coupling=0.5 * sz,
         alpha=0.08, zeta=1.0, wc=4.0, cutoff_type="exponential", T=0.0,
@@ -88,20 +88,20 @@ def cases(oqupy):
         alpha=0.2, zeta=1.0, wc=4.0, cutoff_type="gaussian", T=0.3,
         dt=0.1, dkmax=4, epsrel=1e-7, nsteps=14, rho0=up, add_corr=0.25,
         tempo=True, pt=True)
-    # configs[2]-like strongly coupled, hot instance
+    # strongly coupled, hot instance of the batched spin-boson distribution
     yield "batched_like_hot", dict(
         h=0.5 * 1.5 * sx, gammas=[], lops=[], coupling=0.5 * sz,
         alpha=0.4, zeta=1.0, wc=8.0, cutoff_type="exponential", T=3.0,
         dt=0.05, dkmax=30, epsrel=1e-6, nsteps=60, rho0=up, add_corr=None,
         tempo=True, pt=False)
-    # configs[3]-like qutrit, super-ohmic, GUE Hamiltonian
+    # qutrit, super-ohmic bath, GUE Hamiltonian (batched-qutrit distribution)
     yield "qutrit_superohmic", dict(
         h=_gue(3, rng), gammas=[], lops=[],
         coupling=np.diag([1.0, 0.0, -1.0]), alpha=0.12, zeta=3.0, wc=3.0,
         cutoff_type="exponential", T=1.0, dt=0.05, dkmax=10, epsrel=1e-7,
         nsteps=30, rho0=np.diag([1.0, 0.0, 0.0]).astype(complex),
         add_corr=None, tempo=True, pt=True)
-    # configs[1]-like PT build (reduced memory and length) + dynamics
+    # PT build of the alpha 0.3 / epsrel 1e-7 model (reduced memory and length) + dynamics
     hs = []
     for _ in range(3):
         a, b = rng.uniform(-2, 2, size=2)
