@@ -83,6 +83,170 @@ __device__ __forceinline__ void stage_tile(unsigned char* dst, const __nv_bfloat
   }
 }
 
+// Same tile as stage_tile, with 16-byte cp.async copies (global -> shared,
+// no register round trip) for every aligned full chunk; ragged or unaligned
+// chunks (K % 8 != 0, tile edges) are zero-padded through registers.
+__device__ __forceinline__ void stage_tile_async(unsigned char* dst, const __nv_bfloat16* src, int R, int K,
+                                                 int r0, int k0) {
+  for (int chunk = threadIdx.x; chunk < TC_BM * (TC_BK / 8); chunk += blockDim.x) {
+    const int rr = chunk / (TC_BK / 8), kc = chunk % (TC_BK / 8);
+    const int row = r0 + rr, kk = k0 + kc * 8;
+    const int rg = rr >> 3, r8 = rr & 7;
+    unsigned char* d = dst + (size_t)(rg * (TC_BK / 8) + kc) * 128 + r8 * 16;
+    const __nv_bfloat16* p = src + (size_t)row * K + kk;
+    if (row < R && kk + 8 <= K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(d)), "l"(p) : "memory");
+    } else {
+      union {
+        uint4 u;
+        __nv_bfloat16 h[8];
+      } tmp;
+      tmp.u = make_uint4(0, 0, 0, 0);
+      if (row < R)
+        for (int e = 0; e < 8; ++e)
+          if (kk + e < K) tmp.h[e] = p[e];
+      *reinterpret_cast<uint4*>(d) = tmp.u;
+    }
+  }
+}
+
+__device__ __forceinline__ bool tc_wait_phase(uint64_t* mbar, int phase) {
+  uint32_t done = 0;
+  for (long long it = 0; it < TC_WAIT_LIMIT && !done; ++it) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(phase));
+  }
+  return done != 0;
+}
+
+// Two-stage pipeline version of tc_gemm_kernel: while the tensor core runs
+// the four MMAs of chunk k, the CTA's cp.async copies of chunk k+1 land in
+// the other buffer.  A buffer is refilled only after the mbarrier reports
+// the MMAs that read it complete (at most one MMA batch is outstanding at
+// any wait, so the phase parity identifies it).  All waits are bounded.
+__global__ void __launch_bounds__(TC_THREADS)
+    tc_gemm_pipe_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M, int N,
+                        int K, const float* __restrict__ bias, int epi, const float* __restrict__ zin,
+                        float* __restrict__ zout, float* __restrict__ outf, __nv_bfloat16* __restrict__ outb,
+                        int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_dsm[];
+  unsigned char* sA[2] = {tc_dsm, tc_dsm + TC_BM * TC_BK * 2};
+  unsigned char* sB[2] = {tc_dsm + 2 * TC_BM * TC_BK * 2, tc_dsm + 2 * TC_BM * TC_BK * 2 + TC_BN * TC_BK * 2};
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_err;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TC_BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    s_err = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = make_idesc(TC_BM, TC_BN);
+
+  const int nk = (K + TC_BK - 1) / TC_BK;
+  stage_tile_async(sA[0], A, M, K, m0, 0);
+  stage_tile_async(sB[0], B, N, K, n0, 0);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  int issued = 0;   // MMA batches committed so far (batch j completes phase j & 1)
+  for (int kc = 0; kc < nk; ++kc) {
+    const int buf = kc & 1;
+    if (kc >= 1) {
+      // batch kc - 1 read the other buffer: wait for it before refilling, and
+      // so that no more than one batch is outstanding at any parity wait
+      if (tid == 0 && !s_err && !tc_wait_phase(&mbar, (kc - 1) & 1)) s_err = 1;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      __syncthreads();
+      if (s_err) break;
+    }
+    if (kc + 1 < nk) {
+      stage_tile_async(sA[buf ^ 1], A, M, K, m0, (kc + 1) * TC_BK);
+      stage_tile_async(sB[buf ^ 1], B, N, K, n0, (kc + 1) * TC_BK);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      for (int ks = 0; ks < TC_BK / 16; ++ks) {
+        const uint64_t ad = make_desc(smem_u32(sA[buf]) + ks * 2 * 128, 128, (TC_BK / 8) * 128);
+        const uint64_t bd = make_desc(smem_u32(sB[buf]) + ks * 2 * 128, 128, (TC_BK / 8) * 128);
+        const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar)));
+    }
+    ++issued;
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  // the last committed batch: every earlier one was waited for in the loop
+  if (tid == 0 && !s_err && issued > 0 && !tc_wait_phase(&mbar, (issued - 1) & 1)) s_err = 1;
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  if (!s_err) {
+    const int row = m0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < TC_BN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (row < M) {
+        for (int j = 0; j < 16; ++j) {
+          const int col = n0 + c0 + j;
+          if (col >= N) break;
+          float v = __uint_as_float(r[j]);
+          const size_t o = (size_t)row * N + col;
+          if (epi == EPI_GELU_GRAD) {
+            v *= gelu_grad_f(zin[o]);
+          } else {
+            if (bias) v += bias[col];
+            if (epi == EPI_GELU) {
+              if (zout) zout[o] = v;
+              v = gelu_f(v);
+            }
+          }
+          if (outf) outf[o] = v;
+          if (outb) outb[o] = __float2bfloat16(v);
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+  }
+}
+
 __global__ void __launch_bounds__(TC_THREADS)
     tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M,
                    int N, int K, const float* __restrict__ bias, int epi, const float* __restrict__ zin,
@@ -287,7 +451,15 @@ extern "C" otb_status otb_mlp_gemm(const void* A, const void* B, int32_t M, int3
     return set_error(OTB_ERR_INVALID_ARG, "bad gemm arguments");
   if (epilogue == EPI_GELU_GRAD && !z_in) return set_error(OTB_ERR_INVALID_ARG, "gelu-grad needs z_in");
   dim3 grid((N + TC_BN - 1) / TC_BN, (M + TC_BM - 1) / TC_BM);
-  tc_gemm_kernel<<<grid, TC_THREADS, 0, (cudaStream_t)stream>>>(
+  constexpr int smem = 2 * (TC_BM + TC_BN) * TC_BK * 2;   // two A + B stages, 64 KiB
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (!check_cuda(cudaFuncSetAttribute(tc_gemm_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                    "tc gemm smem"))
+      return OTB_ERR_CUDA;
+    attr_set = true;
+  }
+  tc_gemm_pipe_kernel<<<grid, TC_THREADS, smem, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)A, (const __nv_bfloat16*)B, M, N, K, bias, epilogue, z_in, z_out, out_f32,
       (__nv_bfloat16*)out_bf16, err);
   if (!check_cuda(cudaGetLastError(), "tc gemm")) return OTB_ERR_CUDA;
