@@ -637,7 +637,7 @@ def main():
         run_surrogate(args)
         return
 
-    workload = {"workload": "batched TEMPO spin-boson, 512 instances (alpha U[0.01,0.5], "
+    workload = {"workload": f"batched TEMPO spin-boson, {args.instances} instances (alpha U[0.01,0.5], "
                             "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, "
                             "dt 0.05, epsrel 1e-6, 500-step trajectories)",
                 "instances_per_gpu": args.instances,

@@ -1,0 +1,104 @@
+"""The mixed form's QR-preconditioned bond split, restated in numpy (exact
+SVD in place of the double-float Jacobi) and checked against the plain
+truncated SVD: pivoted Householder QR stopped once the trailing block falls
+below min(1e-3 epsrel, 1e-9) |R_00|, the SVD of the k rows of R, the
+dropped block's squared norm added to the tail sums.  The kept rank must be
+the full SVD's and the reconstruction error its truncation error."""
+import numpy as np
+
+from oracle import tempo_oracle as to
+
+
+def qr_truncated_split(A, epsrel):
+    """A (R x N, R >= N) -> (U, S V^H, kept) as the mixed-form kernel forms
+    them (U = A W / s^2 with W = A^H U S)."""
+    X = np.array(A, dtype=np.complex128)
+    R, N = X.shape
+    piv = np.arange(N)
+    cn = np.sum(np.abs(X) ** 2, axis=0)
+    delta = min(1e-3 * epsrel, 1e-9)
+    k, tail2, r00 = N, 0.0, None
+    for i in range(N):
+        p = i + int(np.argmax(cn[i:]))
+        tot = float(cn[i:].sum())
+        if i == 0:
+            r00 = float(cn[p])
+        elif tot < delta * delta * r00:
+            k, tail2 = i, tot
+            break
+        X[:, [i, p]] = X[:, [p, i]]
+        cn[[i, p]] = cn[[p, i]]
+        piv[[i, p]] = piv[[p, i]]
+        x = X[i:, i]
+        nrm = np.linalg.norm(x)
+        a0 = abs(x[0])
+        e = x[0] / a0 if a0 > 0 else 1.0
+        v = x.copy()
+        v[0] = e * (a0 + nrm)
+        beta = 1.0 / (nrm * (nrm + a0)) if nrm > 0 else 0.0
+        X[i:, i + 1:] -= beta * np.outer(v, v.conj() @ X[i:, i + 1:])
+        X[i, i] = -e * nrm
+        X[i + 1:, i] = 0
+        cn[i + 1:] = np.sum(np.abs(X[i + 1:, i + 1:]) ** 2, axis=0)
+    Rk = np.triu(X[:k, :])
+    Z = np.zeros((N, k), dtype=np.complex128)
+    Z[piv, :] = Rk.conj().T                          # Z = P R_k^H
+    u, s, vh = np.linalg.svd(Z, full_matrices=False)
+    W = u * s                                        # Z V: orthogonal columns
+    cum = tail2 + np.cumsum((s ** 2)[::-1])[::-1]
+    kept = max(1, int(np.sum(np.sqrt(cum) > epsrel * s[0])))
+    U = A @ W[:, :kept] / s[:kept] ** 2
+    return U, W[:, :kept].conj().T, kept, k
+
+
+def _check(theta, epsrel=1e-6):
+    A = theta.conj().T if theta.shape[1] > theta.shape[0] else theta
+    U, C, kept, k = qr_truncated_split(A, epsrel)
+    s = np.linalg.svd(A, compute_uv=False)
+    assert kept == to.truncation_rank(s, epsrel)
+    err = np.linalg.norm(U @ C - A) / np.linalg.norm(A)
+    trunc = np.sqrt(np.sum(s[kept:] ** 2)) / np.linalg.norm(A)
+    assert err <= 1.01 * trunc + 1e-12
+    return k, A.shape[1]
+
+
+def test_random_graded_matrices():
+    rng = np.random.default_rng(0)
+    for _ in range(30):
+        m, n = rng.integers(8, 60, size=2)
+        r = min(m, n)
+        sv = np.sort(10.0 ** (-rng.uniform(0, 14, size=r)))[::-1]
+        U = np.linalg.qr(rng.normal(size=(m, r)) + 1j * rng.normal(size=(m, r)))[0]
+        V = np.linalg.qr(rng.normal(size=(n, r)) + 1j * rng.normal(size=(n, r)))[0]
+        _check((U * sv) @ V.conj().T)
+
+
+def test_captured_tempo_bond_splits():
+    """Every zip-up and sweep split of 40 TEMPO steps of a strongly coupled
+    spin-boson instance (matrices captured from the oracle)."""
+    from oqupy_gb300 import bath
+    sx = np.array([[0, 1], [1, 0]], dtype=complex)
+    sz = np.diag([1.0, -1.0]).astype(complex)
+    infl, U = bath.influences(0.4, 1.0, 8.0, "exponential", 3.0, 0.05, 20, 0.5 * sz)
+    p1, p2 = bath.half_step_propagators(0.75 * sx, 0.05)
+    captured = []
+    orig = to.np.linalg.svd
+
+    def rec(a, *args, **kw):
+        if min(a.shape) >= 8:
+            captured.append(np.array(a))
+        return orig(a, *args, **kw)
+
+    to.np.linalg.svd = rec
+    try:
+        o = to.TempoOracle(np.array([1, 0, 0, 0], dtype=complex), lambda dk: infl[dk] if dk >= 0 else None,
+                           U, lambda s: (p1, p2), np.ones(4), np.ones(4), 20, 1e-6)
+        o.initialize()
+        for _ in range(40):
+            o.compute_step()
+    finally:
+        to.np.linalg.svd = orig
+    assert len(captured) > 100
+    ks = [_check(th) for th in captured[::5]]
+    # the rank-revealing cut shrinks the Jacobi problem on these matrices
+    assert np.mean([k / n for k, n in ks]) < 0.95
