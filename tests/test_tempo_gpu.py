@@ -2,6 +2,8 @@
 
 Every call goes through the C ABI (liboqupy_gb300.so)."""
 
+import json
+
 import numpy as np
 import pytest
 
@@ -117,3 +119,27 @@ def test_set_all_propagators_equals_per_instance_setter():
     a.check_status()
     b.check_status()
     np.testing.assert_array_equal(a.states(0, nsteps + 1), b.states(0, nsteps + 1))
+
+
+def test_autotune_picks_a_timed_candidate_and_caches(tmp_path):
+    """The launch-shape autotuner times each candidate on the batch, returns
+    the fastest, caches it per (precision, D, dkmax bucket), and the chosen
+    shape reproduces the reference within the mixed-form parity bar."""
+    from oqupy_gb300 import TempoBatch, autotune
+    g = gc.load("config1_spin_boson")
+    insts = [dict(hs_dim=g["d"], dkmax=g["dkmax"], epsrel=g["epsrel"],
+                  influences=g["tempo_infl"][: g["dkmax"] + 1], prop1=g["prop1"][0],
+                  prop2=g["prop2"][0], rho0=g["rho0"], unitary=g["unitary"])] * 8
+    cache = str(tmp_path / "tune.json")
+    cands = [(256, 2, 88), (128, 4, 36)]
+    res = autotune.tune(insts, precision="mixed", steps=4, candidates=cands, cache=cache)
+    assert [tuple(c) for c, _ in res["timings"]] == cands
+    assert (res["block"], res["ctas_per_sm"], res["smem_kb"]) in cands
+    again = autotune.tune(insts, precision="mixed", steps=4, candidates=cands, cache=cache)
+    assert again == json.loads(json.dumps(res))          # served from the cache
+    a = TempoBatch(insts, precision="mixed", out_cap=11, block=res["block"], smem_kb=res["smem_kb"])
+    a.advance(10)
+    a.check_status()
+    for st in a.states(0, 11):
+        errs = [to.trace_distance(x, y) for x, y in zip(st, g["tempo_states"][:11])]
+        assert not gc.parity_violations(errs, g["tempo_envelope"][:11], gc.MIXED_ABS)
