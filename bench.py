@@ -100,6 +100,25 @@ def _oracle_worker(args):
     return time.perf_counter() - t0
 
 
+def cpu_oracle_latency(inst, warm, steps, threads):
+    """Latency mode: one instance in one process whose BLAS uses ``threads``
+    threads; returns the seconds of its ``steps`` timed steps."""
+    import multiprocessing as mp
+    env_keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    old = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = str(threads)
+    try:
+        with mp.get_context("spawn").Pool(1) as pool:
+            return float(pool.map(_oracle_worker, [(inst, warm, steps)])[0])
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def cpu_oracle_rate(insts, warm, steps, procs):
     """Trajectories/sec of the oracle on ``insts`` (timed steps only) with
     ``procs`` single-threaded worker processes."""
@@ -652,6 +671,9 @@ def main():
         procs = os.cpu_count() or 1
         rate, cpu_s, wall = cpu_oracle_rate(insts, args.warmup, args.steps, procs)
         per_step_ms = cpu_s / procs / args.steps * 1e3
+        # latency mode: the instance with the longest memory alone, BLAS on all cores
+        big = max(insts, key=lambda i: i["dkmax"])
+        lat_s = cpu_oracle_latency(big, args.warmup, args.steps, procs)
         line = {"metric": METRIC, "value": rate, "unit": "trajectories/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -662,7 +684,12 @@ def main():
                                            f"{args.warmup + args.steps}, numpy oracle, one "
                                            f"single-threaded process per core"},
                 "e2e": {"value": rate, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
+                        "d2h_bytes_per_step": 0},
+                "latency_mode": {"value": args.steps / NSTEPS_TRAJ / lat_s, "unit": "trajectories/s",
+                                 "ms_per_step": lat_s / args.steps * 1e3, "threads": procs,
+                                 "sample": f"one instance (dkmax {big['dkmax']}) x steps "
+                                           f"{args.warmup + 1}..{args.warmup + args.steps}, "
+                                           "BLAS threads = all cores"}}
         print(json.dumps(line))
         return
 
