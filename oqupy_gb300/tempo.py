@@ -28,6 +28,20 @@ def super_unitaries(unitary: np.ndarray):
     return np.kron(u, ud.T), np.kron(ud, u.T)
 
 
+def identity_mask(unitaries, d: int) -> np.ndarray:
+    """Per instance: is the coupling eigenbasis the identity (np.allclose
+    semantics, as fold_propagators tests it)?  One vectorised test for a
+    batch of d x d unitaries (None counts as the identity)."""
+    n = len(unitaries)
+    mask = np.array([u is None for u in unitaries], dtype=bool)
+    rest = [i for i in range(n) if not mask[i]]
+    if rest:
+        U = np.stack([np.asarray(unitaries[i], dtype=np.complex128) for i in rest])
+        eye = np.identity(d)
+        mask[rest] = np.all(np.abs(U - eye) <= 1e-8 + 1e-5 * np.abs(eye), axis=(1, 2))
+    return mask
+
+
 def fold_propagators(prop1, prop2, unitary=None):
     """Fold the coupling-eigenbasis rotation that the reference attaches to
     the dk=0 influence tensor (tempo_backend.py:419-424) into the half-step
@@ -178,7 +192,9 @@ class TempoBatch:
         ``set_propagators``."""
         if unitaries is None:
             unitaries = [None] * self.n
-        if len(set(self.D)) == 1 and all(u is None for u in unitaries):
+        uniform = len(set(self.D)) == 1
+        if uniform and identity_mask(unitaries, int(round(np.sqrt(self.D[0])))).all():
+            # identity eigenbases: the fold is the identity, the batch is packed as given
             a = nat.cplx(np.asarray(p1s).reshape(self.n, self.D[0], self.D[0]))
             b = nat.cplx(np.asarray(p2s).reshape(self.n, self.D[0], self.D[0]))
         else:

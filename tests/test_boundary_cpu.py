@@ -72,3 +72,18 @@ def test_create_rejects_bad_arguments(lib_path):
     cfg = nat.TempoConfig(0, 500, 4, 0)     # chi_cap too large
     assert L.otb_tempo_create(ctypes.byref(cfg), 1, arr, ctypes.byref(h)) == nat.OTB_ERR_INVALID_ARG
     assert L.otb_tempo_advance(None, 1, None) == nat.OTB_ERR_INVALID_ARG
+
+
+def test_identity_mask_matches_fold_semantics():
+    """The batched identity test used by set_all_propagators agrees with the
+    per-instance np.allclose test of fold_propagators, so both setters fold
+    exactly the same instances."""
+    from oqupy_gb300.tempo import identity_mask
+    rng = np.random.default_rng(5)
+    us = [None, np.identity(2), np.identity(2) + 5e-9, np.identity(2) + 2e-5,
+          np.array([[0, 1], [1, 0]], dtype=complex)]
+    for _ in range(10):
+        q, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+        us.append(q)
+    want = [u is None or np.allclose(u, np.identity(2)) for u in us]
+    assert identity_mask(us, 2).tolist() == want
