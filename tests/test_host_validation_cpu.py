@@ -1,0 +1,47 @@
+"""Host-side argument checks of the Python layer: rejected before any device
+work, with the exception types the drop-in contract promises (ValueError for
+bad arguments, NotImplementedError for reference features the GPU engine
+routes back to the reference)."""
+import numpy as np
+import pytest
+
+from oqupy_gb300 import GpuPtTempoBackend, GpuTempoBackend, PtBatch, TempoBatch
+
+
+def _tempo_inst():
+    D = 4
+    return dict(hs_dim=2, dkmax=3, epsrel=1e-6, influences=np.ones((4, D, D), complex),
+                prop1=np.eye(D), prop2=np.eye(D), rho0=np.diag([1.0, 0.0]))
+
+
+def test_tempo_batch_rejects_bad_precision_and_empty_batch():
+    with pytest.raises(ValueError):
+        TempoBatch([_tempo_inst()], precision="fp16")
+    with pytest.raises(ValueError):
+        TempoBatch([], precision="mixed")
+
+
+def test_pt_batch_rejects_bad_arguments():
+    inst = dict(hs_dim=2, num_steps=5, dkmax=3, epsrel=1e-6, influences=np.ones((4, 4, 4), complex))
+    with pytest.raises(ValueError):
+        PtBatch([inst], precision="tf32")
+    with pytest.raises(ValueError):
+        PtBatch([])
+    with pytest.raises(ValueError):
+        PtBatch([dict(inst, num_steps=1)])          # min(num_steps, dkmax + 1) < 2
+
+
+def test_gpu_backends_route_unsupported_reference_features():
+    infl = lambda dk: np.ones((4, 4), complex)       # noqa: E731
+    props = lambda step: (np.eye(4), np.eye(4))      # noqa: E731
+    with pytest.raises(NotImplementedError):
+        GpuTempoBackend(np.ones(4), infl, np.eye(2), props, np.ones(4), np.ones(4), 3, 1e-6,
+                        config={"backend": "gb300"}, degeneracy_maps=([0], [0]))
+    with pytest.raises(NotImplementedError):
+        GpuTempoBackend(np.ones(4), infl, np.eye(2), props, 2 * np.ones(4), np.ones(4), 3, 1e-6,
+                        config={"backend": "gb300"})
+    with pytest.raises(NotImplementedError):
+        GpuPtTempoBackend(2, infl, None, np.ones(4), np.ones(4), 5, 3, 1e-6, {"backend": "gb300"},
+                          degeneracy_maps=([0], [0]))
+    with pytest.raises(NotImplementedError):
+        GpuPtTempoBackend(2, infl, None, np.ones(4), np.zeros(4), 5, 3, 1e-6, {"backend": "gb300"})
