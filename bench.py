@@ -9,10 +9,12 @@ rho0 = spin up.  Inputs are synthetic (seeded draws of those distributions).
 One bench step = one TEMPO time step of every instance (one kernel launch).
 ``value`` = instances x timed steps / 500 / timed seconds, i.e. whole
 trajectories per second at the cost of the timed steps; the per-step cost
-grows with the memory window (min(step, dkmax+1) sites), so the timed window
-is stated in ``config``.  The headline form is "mixed" (double-float Jacobi on
-the FP32 pipe, FP64 everything else); the complex128 form runs the same steps
-and the trace distance between the two is reported.
+grows with the memory window (min(step, dkmax+1) sites) and the bonds, so the
+timed window is stated in ``config`` and ``--full-trajectories`` times all 500
+steps.  The headline form is "mixed" (pivoted QR + Jacobi and the
+contractions in double-float on the FP32 pipe, FP64 rank decisions and site
+storage); the complex128 form runs the same steps and the trace distance
+between the two is reported.
 
 ``--impl reference`` times the CPU oracle (a plain-numpy restatement of the
 reference TEMPO backend) on the same workload and steps, on all host cores.

@@ -24,8 +24,10 @@
 // Site tensors (complex128 in both precision forms) live in a per-instance
 // ring of fixed-capacity slots, layout [l][a][r] (row-major).  That layout is
 // also the column-major (a r) x l matrix the right-to-left sweep factorises,
-// so sweep splits need no reshuffle.  The precision forms differ only in the
-// bond split (jacobi.cuh).
+// so sweep splits need no reshuffle.  The precision forms differ in the bond
+// split (jacobi.cuh) and, in the mixed form, in the contractions (theta,
+// U / carry products, absorb), which run in double-float on the FP32 pipe
+// with their operands converted once per element (ff.cuh: ccacc_fma).
 #include <math.h>
 
 #include <cmath>
