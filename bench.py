@@ -669,7 +669,9 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        t_setup = time.perf_counter()
         insts = make_instances(args.instances, seed)
+        setup_s = time.perf_counter() - t_setup
         procs = os.cpu_count() or 1
         rate, cpu_s, wall = cpu_oracle_rate(insts, args.warmup, args.steps, procs)
         per_step_ms = cpu_s / procs / args.steps * 1e3
@@ -687,6 +689,7 @@ def main():
                                            f"single-threaded process per core"},
                 "e2e": {"value": rate, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0},
+                "setup_seconds": setup_s,
                 "latency_mode": {"value": args.steps / NSTEPS_TRAJ / lat_s, "unit": "trajectories/s",
                                  "ms_per_step": lat_s / args.steps * 1e3, "threads": procs,
                                  "sample": f"one instance (dkmax {big['dkmax']}) x steps "
@@ -702,7 +705,9 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     from oqupy_gb300 import _native
+    t_setup = time.perf_counter()
     insts = make_instances(args.instances, seed)
+    setup_s = time.perf_counter() - t_setup        # influences + propagators on the host
     if args.full_trajectories:
         if rank == 0:
             run_full_trajectories(args, insts, workload)
@@ -784,6 +789,7 @@ def main():
                                                     parallelism=f"instances x {world} GPUs"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "gpu_launches": args.steps, "mixed_stats": stats_mixed,
+                "setup_seconds": setup_s,
                 "whole_trajectories": ("value is trajectory-equivalents at the cost of the timed "
                                        "steps; per-step cost grows ~15x over a 500-step trajectory "
                                        "(longer memory windows, larger bonds): whole trajectories "
