@@ -213,14 +213,14 @@ def trace_distance_max(a, b):
     return 0.5 * np.abs(ev).sum(axis=-1)
 
 
-def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_steps=0):
+def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_steps=0, qr_cut=0.0):
     """Warm-up, ``steps`` device-timed steps; then, on a fresh batch advanced
     through the same warm-up, ``e2e_steps`` steps of the same window through
     the plugin path (all propagators host->device in one call, one launch,
     the new states device->host), wall-clock timed."""
     import numpy as np
     from oqupy_gb300 import TempoBatch
-    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + steps + 1)
+    b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + steps + 1, qr_cut=qr_cut)
     stream = torch.cuda.current_stream()
     for _ in range(warm):
         b.advance(1, stream.cuda_stream)
@@ -247,7 +247,8 @@ def run_gpu_form(torch, insts, precision, warm, steps, flush, chi_cap=64, e2e_st
     b.close()
     e2e = None
     if e2e_steps:
-        b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + e2e_steps + 1)
+        b = TempoBatch(insts, precision=precision, chi_cap=chi_cap, out_cap=warm + e2e_steps + 1,
+                       qr_cut=qr_cut)
         for _ in range(warm):
             b.advance(1, stream.cuda_stream)
         torch.cuda.synchronize()
@@ -607,6 +608,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--no-complex128", action="store_true")
     ap.add_argument("--chi-cap", type=int, default=64)
+    ap.add_argument("--qr-cut", type=float, default=0.0,
+                    help="relative cut of the bond split's QR (0 = the precision form's default)")
     ap.add_argument("--full-trajectories", action="store_true",
                     help="time whole 500-step trajectories of the batch (mixed form only)")
     ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit"])
@@ -723,7 +726,7 @@ def main():
     barrier()
     clocks.start()
     t_mixed, ms_mixed, fl_mixed, st_mixed, stats_mixed, e2e_m = run_gpu_form(
-        torch, insts, "mixed", args.warmup, args.steps, flush, args.chi_cap, args.steps)
+        torch, insts, "mixed", args.warmup, args.steps, flush, args.chi_cap, args.steps, args.qr_cut)
     clk = clocks.stop()
     barrier()
     t_mixed_s = max_over_ranks(t_mixed / 1e3, world)

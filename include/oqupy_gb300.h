@@ -40,11 +40,16 @@ typedef int32_t otb_status;
 #define OTB_ERR_NONFINITE (-6)
 #define OTB_ERR_CHI_OVERFLOW (-7)
 
+/* Both forms split every bond of >= 8 columns by a rank-revealing pivoted
+ * Householder QR followed by one-sided Jacobi on the reduced factor, and
+ * keep site tensors in complex128; column norms, the descending sort, the
+ * tail sums and the epsrel rank decision are FP64 in both.
+ * COMPLEX128: QR, Jacobi and every contraction in FP64.
+ * MIXED: QR, Jacobi rotations and the contractions (theta, U / carry
+ * products, absorb) in double-float arithmetic (pairs of floats, ~48
+ * significant bits) on the FP32 pipe; a split whose double-float sweeps do
+ * not settle is finished by FP64 sweeps. */
 #define OTB_PRECISION_COMPLEX128 0
-/* Bond splits: FP32 one-sided Jacobi (rotations accumulated in FP32) as a
- * preconditioner, then B = A V in FP64 and FP64 Jacobi sweeps to
- * convergence; site tensors, contractions, norms, rank decisions and the
- * read-out stay FP64. */
 #define OTB_PRECISION_MIXED 1
 
 /* ------------------------------------------------------------------ TEMPO */
@@ -53,12 +58,18 @@ typedef struct otb_tempo otb_tempo;
 
 typedef struct {
   int32_t precision;   /* OTB_PRECISION_* */
-  int32_t chi_cap;     /* bond-dimension capacity of every site (<= 128) */
+  int32_t chi_cap;     /* bond-dimension capacity of every site, chi_cap * D <= 1152 */
   int32_t out_cap;     /* states kept per instance (ring), >= 2 */
   int32_t grid;        /* CTAs per launch, 0 = 3 per SM */
   int32_t block;       /* threads per CTA (64..256, multiple of 32), 0 = 256 */
   int32_t smem_kb;     /* dynamic shared memory per CTA for working matrices
                           (KiB, <= 200), 0 = 56 */
+  double qr_cut;       /* relative cut of the rank-revealing QR that precedes
+                          the Jacobi SVD of every split of >= 8 columns: the
+                          factorisation stops once the remaining block's
+                          Frobenius norm is below qr_cut * |R_00| (its squared
+                          norm joins the truncation tail).  0 = default:
+                          1e-14 (complex128), min(1e-3 epsrel, 1e-9) (mixed) */
 } otb_tempo_config;
 
 typedef struct {
@@ -139,6 +150,7 @@ typedef struct {
   int32_t precision;   /* OTB_PRECISION_* */
   int32_t chi_cap;     /* bond-dimension capacity of every site, chi_cap * D <= 1152 */
   int32_t grid;        /* CTAs per launch, 0 = 2 per SM */
+  double qr_cut;       /* as otb_tempo_config.qr_cut (0 = default) */
 } otb_pt_config;
 
 typedef struct {
@@ -208,13 +220,25 @@ otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t n_systems,
  * (1 MiB, present on every GPU that loads the library until exit), which
  * limits bonds to chi_cap * D <= OTB_TEMPO_STATIC_MAX_CHI_D.
  *
- * One instance, one CTA.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and should therefore come before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race, so issue them on one stream (or otherwise serialise them).  Nothing
- * in the array needs to start at zero.  The MPS buffer must be zeroed by the
- * caller before the first call; it then carries the instance between calls.
- * The function calls no cudaMalloc or cudaFree. */
+ * One instance, one CTA.  Every call looks up the array's device address
+ * for the current device and context (cudaGetSymbolAddress, which allocates
+ * nothing); the first call on a device also loads the library's kernels
+ * there and should therefore come before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race, so issue them on one
+ * stream (or otherwise serialise them).  Nothing in the array needs to
+ * start at zero.  The MPS buffer must be zeroed by the caller before the
+ * first call; it then carries the instance between calls.  The function
+ * calls no cudaMalloc or cudaFree.
+ *
+ * Failures inside a step (a bond beyond chi_cap, a split that does not
+ * converge, a non-finite value) are reported through status_out, written
+ * on the stream by every call: [0] status (0 or a negative otb_status),
+ * [1] steps completed by this call = rows of states_out written (the rest
+ * are left untouched), [2] steps completed by the instance in total,
+ * [3] largest bond dimension after the last completed step.  After a
+ * nonzero status the MPS buffer holds a partly updated step: later calls
+ * complete no step and report the same status until the caller zeroes the
+ * buffer, which restarts the instance from rho0. */
 #define OTB_TEMPO_STATIC_MAX_CHI_D 128
 /* bytes of the MPS buffer: state header, dims, (dkmax+2) site slots */
 #define OTB_TEMPO_STATIC_MPS_BYTES(hs_dim, dkmax, chi_cap)                          \
@@ -235,6 +259,7 @@ typedef struct {
                                 the first call */
   int64_t mps_bytes;
   double* states_out;        /* device: nsteps * D complex, states of this call's steps */
+  int32_t* status_out;       /* device: 4 int32 (see above), written by every call */
 } otb_tempo_static_io;
 
 /* Advance one TEMPO instance by nsteps without allocating. */

@@ -14,6 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboqupy_gb300.so")
 
 OTB_OK = 0
+# largest bond split (columns) one CTA handles: chi_cap * D <= MAX_COLUMNS
+MAX_COLUMNS = 1152
+
 OTB_ERR_INVALID_ARG = -1
 OTB_ERR_OOM = -2
 OTB_ERR_CUDA = -3
@@ -41,7 +44,8 @@ c_int32_p = ctypes.POINTER(ctypes.c_int32)
 class TempoConfig(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("chi_cap", ctypes.c_int32),
                 ("out_cap", ctypes.c_int32), ("grid", ctypes.c_int32),
-                ("block", ctypes.c_int32), ("smem_kb", ctypes.c_int32)]
+                ("block", ctypes.c_int32), ("smem_kb", ctypes.c_int32),
+                ("qr_cut", ctypes.c_double)]
 
 
 class TempoInstance(ctypes.Structure):
@@ -62,7 +66,7 @@ class TempoInfo(ctypes.Structure):
 
 class PtConfig(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("chi_cap", ctypes.c_int32),
-                ("grid", ctypes.c_int32)]
+                ("grid", ctypes.c_int32), ("qr_cut", ctypes.c_double)]
 
 
 class PtInstance(ctypes.Structure):

@@ -65,6 +65,8 @@ extern "C" otb_status otb_pt_create(const otb_pt_config* cfg, int32_t n, const o
     return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be in [4, 1152 / D]");
   std::unique_ptr<otb_pt> h(new otb_pt());
   h->n = n;
+  if (!(cfg->qr_cut >= 0.0) || !(cfg->qr_cut < 1.0))
+    return set_error(OTB_ERR_INVALID_ARG, "qr_cut must be in [0, 1)");
   h->precision = cfg->precision;
   h->cap = cfg->chi_cap;
   h->inst.resize(n);
@@ -90,6 +92,7 @@ extern "C" otb_status otb_pt_create(const otb_pt_config* cfg, int32_t n, const o
     I.num_infl = num_infl;
     I.cap = h->cap;
     I.epsrel = s.epsrel;
+    I.qr_delta = (float)cfg->qr_cut;
     I.has_neg = s.neg_influences ? 1 : 0;
     I.site_base = site_total;
     site_total += (long long)s.num_steps * h->cap * D * h->cap;

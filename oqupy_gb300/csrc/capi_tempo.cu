@@ -134,13 +134,15 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   *out = nullptr;
   if (cfg->precision != OTB_PRECISION_COMPLEX128 && cfg->precision != OTB_PRECISION_MIXED)
     return set_error(OTB_ERR_INVALID_ARG, "precision must be 0 (complex128) or 1 (mixed)");
-  if (cfg->chi_cap < 4 || cfg->chi_cap > 128)
-    return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be in [4, 128]");
+  if (cfg->chi_cap < 4 || cfg->chi_cap > 1152)
+    return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be in [4, 1152 / D]");
   if (cfg->out_cap < 2) return set_error(OTB_ERR_INVALID_ARG, "out_cap must be >= 2");
   if (cfg->block != 0 && (cfg->block < 64 || cfg->block > 256 || cfg->block % 32 != 0))
     return set_error(OTB_ERR_INVALID_ARG, "block must be 0 or a multiple of 32 in [64, 256]");
   if (cfg->smem_kb < 0 || cfg->smem_kb > 200)
     return set_error(OTB_ERR_INVALID_ARG, "smem_kb must be in [0, 200]");
+  if (!(cfg->qr_cut >= 0.0) || !(cfg->qr_cut < 1.0))
+    return set_error(OTB_ERR_INVALID_ARG, "qr_cut must be in [0, 1)");
   std::unique_ptr<otb_tempo> h(new otb_tempo());
   h->block = cfg->block > 0 ? cfg->block : 256;
   h->smem_bytes = cfg->smem_kb * 1024;
@@ -160,6 +162,7 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
       return set_error(OTB_ERR_INVALID_ARG, "hs_dim must be 1..3 (Liouville dimension <= 9)");
     const int D = s.hs_dim * s.hs_dim;
     if (D > h->cap) return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be >= D");
+    if (D * h->cap > 1152) return set_error(OTB_ERR_INVALID_ARG, "chi_cap * D must be <= 1152");
     if (!(s.epsrel > 0.0) || !std::isfinite(s.epsrel))
       return set_error(OTB_ERR_INVALID_ARG, "epsrel must be positive and finite");
     if (!s.influences || !s.prop1 || !s.prop2 || !s.rho0)
@@ -175,6 +178,7 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     I.dkmax = full ? (1 << 29) : s.dkmax;
     I.cap = h->cap;
     I.epsrel = s.epsrel;
+    I.qr_delta = (float)cfg->qr_cut;
     I.out_cap = h->out_cap;
     I.out_origin = 0;
     const int want = full ? std::max(s.max_sites, 8) : s.dkmax + 2;

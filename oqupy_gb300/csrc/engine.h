@@ -13,6 +13,7 @@ struct InstDev {
   int cap;           // bond-dimension capacity of every site slot
   int nslots;        // ring slots for MPS sites (>= sites + 1)
   double epsrel;     // relative truncation tolerance
+  float qr_delta;    // relative cut of the split's QR (<= 0: default by precision)
   long long site_base;   // element offset of slot 0 in the site arena
   long long dims_base;   // int2 offset of slot 0 in the dims array
   long long infl_base;   // element offset of influence dk=0 (D*D each, row-major [a][r])
@@ -78,6 +79,7 @@ struct PtDev {
   int cap;            // bond-dimension capacity per site
   int has_neg;        // grow-phase influences for dk = -step supplied
   double epsrel;
+  float qr_delta;     // relative cut of the split's QR (<= 0: default by precision)
   long long site_base;  // num_steps slots of cap * D * cap
   long long dims_base;  // num_steps int2
   long long infl_base;  // num_infl * D * D, dk = 0 .. num_infl-1

@@ -21,9 +21,8 @@
 //  * mixed, small splits (jacobi_truncate_mixed): the same sweeps in
 //    double-float arithmetic (ff.cuh) on the FP32 pipe, FP64 fallback sweeps
 //    if they do not settle;
-//  * mixed (jacobi_truncate_mixed_qr, >= 8 columns): rank-revealing pivoted
-//    Householder QR in double-float, then the double-float sweeps on the k
-//    rows of R (described above the function).
+//  * both forms, >= 8 columns: rank-revealing pivoted Householder QR, then
+//    these sweeps on the k rows of R (qr.cuh).
 #pragma once
 
 #include "common.cuh"
@@ -35,12 +34,6 @@ constexpr int JACOBI_MAX_SWEEPS = 60;
 
 struct JacobiShared {
   double red[33];
-  float qv[32];     // QR pivot search: per-warp best value, sum and index
-  float qs[32];
-  int qi[32];
-  float q_r00;      // |R_00|^2 of the pivoted QR
-  float q_tot;      // remaining squared mass at the current QR step
-  int q_piv;        // pivot column of the current QR step
   int flag[2];
   float worst[2];   // largest relative off-diagonal rotated in a sweep
   int noise_converged;
@@ -478,250 +471,6 @@ __device__ inline int jacobi_truncate_mixed(cx<double>* W, int m, int n, cff* Wf
   const int kk = jacobi_finish<double>(W, m, n, m, epsrel, norm, perm, sh, ff_done ? 0 : sw64);
   if (threadIdx.x == 0) sh->sweeps = ff_done ? 0 : sw64;
   __syncthreads();
-  return kk;
-}
-
-// ---------------------------------------------------------------------------
-// Mixed driver with a rank-revealing QR preconditioner.
-//
-// The oriented matrix A (R x N, R >= N) is factorised A P = Q R by Householder
-// QR with column pivoting in double-float arithmetic, stopped at the first step
-// k whose trailing block has Frobenius norm below delta |R_00|.  One-sided
-// Jacobi then runs on Z = P R[0:k, :]^H (N x k): its columns converge in far
-// fewer sweeps than those of A (the pivoted R is already graded), and there are
-// only k of them.  With Z V = W orthogonal,  A ~= (Q V) Sigma (W / Sigma)^H, so
-// W = A^H U Sigma / Sigma = V_A Sigma: the result is the conjugate-side factor
-// of A (N x k, leading dimension N).  The dropped block's squared norm belongs
-// to the tail of every kept index and is added to the tail sums, so the rank
-// decision equals the one of the full decomposition up to delta.
-// ---------------------------------------------------------------------------
-
-// Householder QR with column pivoting of X (R x N, FF, column-major ld R),
-// stopped as described above.  On return the upper trapezoid X[0:k, 0:N]
-// holds R in pivoted column order, piv[p] is the original column of pivoted
-// position p, *tail2 the squared Frobenius norm of the dropped block.
-__device__ inline int ff_qrcp(cff* X, int Rr, int N, float delta, int* piv, float* cn, JacobiShared* sh,
-                              float* tail2) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane32 = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  for (int j = warp; j < N; j += nw) {
-    float acc = 0.f;
-    const cff* c = X + (size_t)j * Rr;
-    for (int r = lane32; r < Rr; r += 32) acc = fmaf(c[r].x.hi, c[r].x.hi, fmaf(c[r].y.hi, c[r].y.hi, acc));
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (lane32 == 0) {
-      cn[j] = acc;
-      piv[j] = j;
-    }
-  }
-  __syncthreads();
-  int k = N;
-  *tail2 = 0.f;
-  for (int i = 0; i < N; ++i) {
-    // (a) pivot: largest remaining partial column norm; total remaining mass
-    float bv = -1.f, sum = 0.f;
-    int bi = i;
-    for (int j = i + tid; j < N; j += nt) {
-      const float v = cn[j];
-      sum += v;
-      if (v > bv) {
-        bv = v;
-        bi = j;
-      }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, off);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (ov > bv || (ov == bv && oi < bi)) {
-        bv = ov;
-        bi = oi;
-      }
-      sum += __shfl_xor_sync(0xffffffffu, sum, off);
-    }
-    if (lane32 == 0) {
-      sh->qv[warp] = bv;
-      sh->qi[warp] = bi;
-      sh->qs[warp] = sum;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      float b = sh->qv[0], tot = sh->qs[0];
-      int ib = sh->qi[0];
-      for (int w = 1; w < nw; ++w) {
-        tot += sh->qs[w];
-        if (sh->qv[w] > b || (sh->qv[w] == b && sh->qi[w] < ib)) {
-          b = sh->qv[w];
-          ib = sh->qi[w];
-        }
-      }
-      if (i == 0) sh->q_r00 = b;
-      sh->q_piv = ib;
-      sh->q_tot = tot;
-      sh->kept = (i > 0 && tot < delta * delta * sh->q_r00) ? 1 : 0;
-    }
-    __syncthreads();
-    if (sh->kept) {
-      k = i;
-      *tail2 = sh->q_tot;
-      break;
-    }
-    const int p = sh->q_piv;
-    // (b) swap columns i and p
-    if (p != i) {
-      cff* ci = X + (size_t)i * Rr;
-      cff* cp = X + (size_t)p * Rr;
-      for (int r = tid; r < Rr; r += nt) {
-        const cff t = ci[r];
-        ci[r] = cp[r];
-        cp[r] = t;
-      }
-      if (tid == 0) {
-        const float t = cn[i];
-        cn[i] = cn[p];
-        cn[p] = t;
-        const int q = piv[i];
-        piv[i] = piv[p];
-        piv[p] = q;
-      }
-    }
-    __syncthreads();
-    // (c) Householder vector of column i (rows i..R-1); scalars in FP64
-    {
-      cff* ci = X + (size_t)i * Rr;
-      ff acc = ff_make(0.f, 0.f);
-      for (int r = i + tid; r < Rr; r += nt) {
-        const cff x = ci[r];
-        acc = ff_fma(x.x, x.x, ff_fma(x.y, x.y, acc));
-      }
-      for (int off = 16; off > 0; off >>= 1) acc = ff_add(acc, ff_shfl_xor(acc, off));
-      if (lane32 == 0) sh->red[warp] = ff_to(acc);
-      __syncthreads();
-      if (tid == 0) {
-        double n2 = 0.0;
-        for (int w = 0; w < nw; ++w) n2 += sh->red[w];
-        const double nrm = sqrt(n2);
-        const cx<double> x0 = cff_to(ci[i]);
-        const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
-        const cx<double> e = (a0 > 0.0) ? mk<double>(x0.x / a0, x0.y / a0) : mk<double>(1.0, 0.0);
-        // H = I - beta v v^H with v = x - alpha e_i, alpha = -e |x|, v_i = e (|x_i| + |x|)
-        sh->red[0] = e.x * (a0 + nrm);
-        sh->red[1] = e.y * (a0 + nrm);
-        sh->red[2] = (nrm > 0.0) ? 1.0 / (nrm * (nrm + a0)) : 0.0;
-        sh->red[3] = -e.x * nrm;
-        sh->red[4] = -e.y * nrm;
-        ci[i] = cff_from(mk<double>(sh->red[0], sh->red[1]));
-      }
-      __syncthreads();
-    }
-    // (d) apply H to columns i+1..N-1 and refresh their partial norms (rows > i)
-    {
-      const ff fbeta = ff_from(sh->red[2]);
-      const cff* v = X + (size_t)i * Rr;
-      const int G = jacobi_group(Rr - i);
-      const int lane = tid & (G - 1), group = tid / G, ngroups = nt / G;
-      for (int jb = i + 1; jb < N; jb += ngroups) {
-        const int j = jb + group;
-        const bool act = j < N;
-        ff wr = ff_make(0.f, 0.f), wi = wr;
-        cff* cj = X + (size_t)(act ? j : i) * Rr;
-        if (act) {
-          for (int r = i + lane; r < Rr; r += G) {
-            const cff a = v[r], x = cj[r];
-            // w += conj(v_r) x_r
-            wr = ff_fma(a.x, x.x, ff_fma(a.y, x.y, wr));
-            wi = ff_fma(a.x, x.y, ff_sub(wi, ff_mul(a.y, x.x)));
-          }
-        }
-        for (int off = G >> 1; off > 0; off >>= 1) {
-          wr = ff_add(wr, ff_shfl_xor(wr, off));
-          wi = ff_add(wi, ff_shfl_xor(wi, off));
-        }
-        float s2 = 0.f;
-        if (act) {
-          const ff bx = ff_mul(fbeta, wr), by = ff_mul(fbeta, wi);
-          for (int r = i + lane; r < Rr; r += G) {
-            const cff a = v[r];
-            cff x = cj[r];
-            // x -= v_r (beta w)
-            x.x = ff_sub(x.x, ff_sub(ff_mul(a.x, bx), ff_mul(a.y, by)));
-            x.y = ff_sub(x.y, ff_add(ff_mul(a.x, by), ff_mul(a.y, bx)));
-            cj[r] = x;
-            if (r > i) s2 = fmaf(x.x.hi, x.x.hi, fmaf(x.y.hi, x.y.hi, s2));
-          }
-        }
-        for (int off = G >> 1; off > 0; off >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, off, 32);
-        if (act && lane == 0) cn[j] = s2;
-      }
-      __syncthreads();
-      if (tid == 0) X[(size_t)i * Rr + i] = cff_from(mk<double>(sh->red[3], sh->red[4]));
-      __syncthreads();
-    }
-  }
-  __syncthreads();
-  return k;
-}
-
-// Mixed driver with the QR preconditioner.  W (R x N, FP64, ld R) holds the
-// oriented matrix and is used as scratch; X (R x N, FF) is the QR workspace;
-// zs / zs_bytes is spare shared memory for the Jacobi operand.  Returns the
-// kept rank; *Wout (FP64, N x k, ld N, in X's storage) holds V_A Sigma with
-// norm / perm describing its columns as in jacobi_finish.
-__device__ inline int jacobi_truncate_mixed_qr(cx<double>* W, int R, int N, cff* X, unsigned char* zs,
-                                               size_t zs_bytes, double epsrel, double* norm, int* perm,
-                                               JacobiShared* sh, cx<double>** Wout) {
-  const int tid = threadIdx.x;
-  const int nt = blockDim.x;
-  double mx = 0.0;
-  for (int idx = tid; idx < R * N; idx += nt) mx = fmax(mx, fmax(fabs(W[idx].x), fabs(W[idx].y)));
-  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-  if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
-  __syncthreads();
-  if (tid == 0) {
-    double v = 0.0;
-    for (int w = 0; w < nt / 32; ++w) v = fmax(v, sh->red[w]);
-    sh->red[32] = (v > 0.0) ? v : 1.0;
-  }
-  __syncthreads();
-  const double scale = sh->red[32];
-  const double inv = 1.0 / scale;
-  for (int idx = tid; idx < R * N; idx += nt) X[idx] = cff_from(cscale(W[idx], inv));
-  __syncthreads();
-  // QR with pivoting; cn and the inverse permutation live in norm[] (free until the finish)
-  float* cn = reinterpret_cast<float*>(norm);
-  int* pinv = reinterpret_cast<int*>(norm) + N;
-  const float delta = (float)fmin(1e-3 * epsrel, 1e-9);
-  float tail2;
-  const int k = ff_qrcp(X, R, N, delta, perm, cn, sh, &tail2);
-  for (int p = tid; p < N; p += nt) pinv[perm[p]] = p;
-  __syncthreads();
-  // Z = P R[0:k, :]^H: row q (original column q of A), column i
-  cff* Z = ((size_t)N * k * sizeof(cff) <= zs_bytes) ? reinterpret_cast<cff*>(zs) : reinterpret_cast<cff*>(W);
-  for (int idx = tid; idx < N * k; idx += nt) {
-    const int i = idx / N, q = idx - i * N;
-    const int pos = pinv[q];
-    cff z;
-    if (pos >= i) {
-      z = X[(size_t)pos * R + i];  // conj(R[i][pos])
-      z.y.hi = -z.y.hi;
-      z.y.lo = -z.y.lo;
-    } else {
-      z.x = ff_make(0.f, 0.f);
-      z.y = z.x;
-    }
-    Z[idx] = z;
-  }
-  __syncthreads();
-  const int sw = jacobi_sweeps_ff(Z, N, k, N, sh);
-  const bool ff_done = sw < JACOBI_MAX_SWEEPS || sh->noise_converged;
-  cx<double>* O = reinterpret_cast<cx<double>*>(X);
-  for (int idx = tid; idx < N * k; idx += nt) O[idx] = cscale(cff_to(Z[idx]), scale);
-  __syncthreads();
-  const int sw64 = ff_done ? 0 : jacobi_sweeps<double>(O, N, k, N, nullptr, 0, sh);
-  if (tid == 0) sh->sweeps32 = sw;
-  const int kk = jacobi_finish<double>(O, N, k, N, epsrel, norm, perm, sh, ff_done ? 0 : sw64,
-                                       (double)tail2 * scale * scale);
-  if (tid == 0) sh->sweeps = ff_done ? 0 : sw64;
-  __syncthreads();
-  *Wout = O;
   return kk;
 }
 

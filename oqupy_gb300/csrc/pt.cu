@@ -70,7 +70,7 @@ __device__ void sweep_rl(PtCtx<MIXED>& c, PtShared& sh, int k) {
   const int l = c.dims[k].x, r = c.dims[k].y;
   const int m = D * r, n = l;
   ColMajor X{A, m};
-  const int kk = split_generic<MIXED>(X, m, n, c.I->epsrel, c.I->cap, c.b, sh.ssh, &sh.st.status,
+  const int kk = split_generic<MIXED>(X, m, n, c.I->epsrel, c.I->qr_delta, c.I->cap, c.b, sh.ssh, &sh.st.status,
                                       &sh.st.sweeps64, &sh.st.sweepsff, &sh.st.flops_alg);
   if (kk == 0) return;
   for (int idx = tid; idx < m * kk; idx += nt) A[idx] = c.b.Tg[idx];
@@ -105,7 +105,7 @@ __device__ void sweep_lr(PtCtx<MIXED>& c, PtShared& sh, int k) {
   const int l = c.dims[k].x, r = c.dims[k].y;
   const int m = l * D, n = r;
   RowMajor X{A, r};
-  const int kk = split_generic<MIXED>(X, m, n, c.I->epsrel, c.I->cap, c.b, sh.ssh, &sh.st.status,
+  const int kk = split_generic<MIXED>(X, m, n, c.I->epsrel, c.I->qr_delta, c.I->cap, c.b, sh.ssh, &sh.st.status,
                                       &sh.st.sweeps64, &sh.st.sweepsff, &sh.st.flops_alg);
   if (kk == 0) return;
   // U (m x kk, column-major in Tg) -> site [l][a][j]
@@ -255,7 +255,7 @@ __device__ void pt_step(PtCtx<MIXED>& c, PtShared& sh) {
       break;
     }
     ColMajor X{c.Xg, m};
-    const int kk = split_generic<MIXED>(X, m, n, I.epsrel, I.cap, c.b, sh.ssh, &sh.st.status,
+    const int kk = split_generic<MIXED>(X, m, n, I.epsrel, I.qr_delta, I.cap, c.b, sh.ssh, &sh.st.status,
                                         &sh.st.sweeps64, &sh.st.sweepsff, &sh.st.flops_alg);
     if (kk == 0) return;
     // U((x,a), j) -> site [j][a][x]

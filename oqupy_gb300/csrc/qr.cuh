@@ -1,0 +1,343 @@
+// Rank-revealing QR preconditioner + one-sided Jacobi on the reduced factor:
+// the truncated bond split of both precision forms for splits of >= 8
+// columns (smaller splits run plain Jacobi, jacobi.cuh).
+//
+// Replaces, like jacobi.cuh, the truncated SVD that the reference obtains
+// from tensornetwork's split_node_full_svd(max_truncation_err=epsrel,
+// relative=True) (oqupy/backends/node_array.py:262-268, 285-291, 541-547),
+// with the rank rule chi = #{i : sqrt(sum_{j>=i} s_j^2) > epsrel * s_0}
+// (oqupy/mps_mpo.py:452-457).
+//
+// The oriented matrix A (R x N, R >= N) is factorised A P = Q R by
+// Householder QR with column pivoting, stopped at the first step k whose
+// remaining block has Frobenius norm below delta |R_00|.  One-sided Jacobi
+// then orthogonalises the columns of Z = P R[0:k, :]^H (N x k): the pivoted
+// R is graded, so Z converges in few sweeps, and it has only k columns.
+// With Z V = W orthogonal, A ~= (Q V) Sigma (W / Sigma)^H, so W = A^H U Sigma:
+// the caller receives the conjugate-side factor (N x k, ld N).  The dropped
+// block's squared norm belongs to the tail of every kept index and is added
+// to the tail sums, so the rank decision is that of the full decomposition up
+// to delta.
+//
+// Arithmetic (template parameter T):
+//   double -- complex128 form: FP64 throughout; delta at the factorisation's
+//             own backward-error level (1e-14 by default);
+//   ff     -- mixed form: double-float (ff.cuh) on the FP32 pipe; delta
+//             min(1e-3 epsrel, 1e-9) by default.
+// Norms, the descending sort, the tail sums and the rank decision are FP64 in
+// both (jacobi_finish).
+//
+// Synchronisation: one __syncthreads per QR column.  No columns are
+// exchanged: column p_i chosen at step i keeps its storage; a short list of
+// the unchosen columns is exchanged instead.  The pivot, the remaining mass
+// and the reflector scalars are computed redundantly by every warp from data
+// no thread writes during the step (partial norms and the column list are
+// double-buffered by step parity; the diagonal R_ii is stored one step late,
+// when no warp reads that column any more).
+#pragma once
+
+#include "jacobi.cuh"
+
+namespace otb {
+
+template <typename T>
+struct QA;
+
+template <>
+struct QA<double> {
+  typedef cx<double> E;  // element of the working matrix
+  typedef double S;      // accurate real scalar
+  static constexpr bool kFF = false;
+  static __device__ __forceinline__ E from(cx<double> z) { return z; }
+  static __device__ __forceinline__ cx<double> to(const E& e) { return e; }
+  static __device__ __forceinline__ S zero() { return 0.0; }
+  static __device__ __forceinline__ S fromd(double d) { return d; }
+  static __device__ __forceinline__ double tod(S s) { return s; }
+  static __device__ __forceinline__ S add(S a, S b) { return a + b; }
+  static __device__ __forceinline__ S mul(S a, S b) { return a * b; }
+  static __device__ __forceinline__ S shfl(S v, int off) { return __shfl_xor_sync(0xffffffffu, v, off, 32); }
+  static __device__ __forceinline__ S abs2_acc(const E& x, S acc) { return fma(x.x, x.x, fma(x.y, x.y, acc)); }
+  static __device__ __forceinline__ float abs2f(const E& x) { return (float)fma(x.x, x.x, x.y * x.y); }
+  // (wr, wi) += conj(a) x
+  static __device__ __forceinline__ void dotj(S& wr, S& wi, const E& a, const E& x) {
+    wr = fma(a.x, x.x, fma(a.y, x.y, wr));
+    wi = fma(a.x, x.y, fma(-a.y, x.x, wi));
+  }
+  // x - a (bx + i by)
+  static __device__ __forceinline__ E sub_scaled(const E& x, const E& a, S bx, S by) {
+    return mk<double>(x.x - fma(a.x, bx, -a.y * by), x.y - fma(a.x, by, a.y * bx));
+  }
+  static __device__ __forceinline__ E conj(const E& x) { return mk<double>(x.x, -x.y); }
+  static __device__ __forceinline__ E zeroE() { return mk<double>(0.0, 0.0); }
+};
+
+template <>
+struct QA<ff> {
+  typedef cff E;
+  typedef ff S;
+  static constexpr bool kFF = true;
+  static __device__ __forceinline__ E from(cx<double> z) { return cff_from(z); }
+  static __device__ __forceinline__ cx<double> to(const E& e) { return cff_to(e); }
+  static __device__ __forceinline__ S zero() { return ff_make(0.f, 0.f); }
+  static __device__ __forceinline__ S fromd(double d) { return ff_from(d); }
+  static __device__ __forceinline__ double tod(S s) { return ff_to(s); }
+  static __device__ __forceinline__ S add(S a, S b) { return ff_add(a, b); }
+  static __device__ __forceinline__ S mul(S a, S b) { return ff_mul(a, b); }
+  static __device__ __forceinline__ S shfl(S v, int off) { return ff_shfl_xor(v, off); }
+  static __device__ __forceinline__ S abs2_acc(const E& x, S acc) { return ff_fma(x.x, x.x, ff_fma(x.y, x.y, acc)); }
+  static __device__ __forceinline__ float abs2f(const E& x) { return fmaf(x.x.hi, x.x.hi, x.y.hi * x.y.hi); }
+  static __device__ __forceinline__ void dotj(S& wr, S& wi, const E& a, const E& x) {
+    wr = ff_fma(a.x, x.x, ff_fma(a.y, x.y, wr));
+    wi = ff_fma(a.x, x.y, ff_sub(wi, ff_mul(a.y, x.x)));
+  }
+  static __device__ __forceinline__ E sub_scaled(const E& x, const E& a, S bx, S by) {
+    E r;
+    r.x = ff_sub(x.x, ff_sub(ff_mul(a.x, bx), ff_mul(a.y, by)));
+    r.y = ff_sub(x.y, ff_add(ff_mul(a.x, by), ff_mul(a.y, bx)));
+    return r;
+  }
+  static __device__ __forceinline__ E conj(const E& x) {
+    E r = x;
+    r.y.hi = -r.y.hi;
+    r.y.lo = -r.y.lo;
+    return r;
+  }
+  static __device__ __forceinline__ E zeroE() {
+    E r;
+    r.x = ff_make(0.f, 0.f);
+    r.y = r.x;
+    return r;
+  }
+};
+
+// Default relative cut of the QR (the remaining block's Frobenius norm over
+// |R_00|) for each arithmetic.
+__device__ __forceinline__ float qr_default_delta(bool ffarith, double epsrel) {
+  return ffarith ? (float)fmin(1e-3 * epsrel, 1e-9) : 1e-14f;
+}
+
+// Householder QR with column pivoting of X (R x N, column-major ld R), in
+// place, without column exchanges.  Workspace: cn holds 2 N floats (partial
+// squared column norms by column, double-buffered by step parity), lists
+// 2 N shorts (by step parity: positions 0..i-1 the columns chosen at steps
+// 0..i-1, positions i..N-1 the unchosen ones).  Returns k and writes
+// colstep[j] (N ints, in cn's storage, valid after the call) = the step at
+// which column j was chosen, N for never; for i < k, X[j * R + i] = R[i][j]
+// for every column j with colstep[j] >= i (colstep[j] == i: the diagonal of
+// step i).  *tail2 is the remaining squared mass at the stop (0 when all N
+// steps ran).
+template <typename T>
+__device__ int qrcp_inplace(typename QA<T>::E* X, int R, int N, float delta, float* cn, short* lists,
+                            float* tail2) {
+  typedef QA<T> Q;
+  typedef typename Q::E E;
+  typedef typename Q::S S;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane32 = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int j = warp; j < N; j += nw) {
+    float acc = 0.f;
+    const E* c = X + (size_t)j * R;
+    for (int r = lane32; r < R; r += 32) acc += Q::abs2f(c[r]);
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane32 == 0) cn[j] = acc;
+  }
+  for (int j = tid; j < N; j += nt) lists[j] = (short)j;
+  __syncthreads();
+  float r00 = 0.f, t2 = 0.f;
+  int k = N;
+  int pend_p = -1;  // thread 0: column and value of the previous step's diagonal
+  E pend_a = Q::zeroE();
+  for (int i = 0; i < N; ++i) {
+    const float* cur = cn + (i & 1) * N;
+    float* nxt = cn + ((i + 1) & 1) * N;
+    const short* Lc = lists + (i & 1) * N;
+    short* Ln = lists + ((i + 1) & 1) * N;
+    // (a) pivot (largest partial norm, lowest list position on ties) and
+    // remaining mass over the unchosen columns, by every warp; the xor
+    // butterfly leaves bitwise-identical results in every lane, and every
+    // warp reduces the same data in the same order
+    float bv = -1.f, sum = 0.f;
+    int bq = N;
+    for (int q = i + lane32; q < N; q += 32) {
+      const float v = cur[Lc[q]];
+      sum += v;
+      if (v > bv) {
+        bv = v;
+        bq = q;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, off);
+      const int oq = __shfl_xor_sync(0xffffffffu, bq, off);
+      if (ov > bv || (ov == bv && oq < bq)) {
+        bv = ov;
+        bq = oq;
+      }
+      sum += __shfl_xor_sync(0xffffffffu, sum, off);
+    }
+    if (i == 0) {
+      r00 = bv;
+    } else if (sum < delta * delta * r00) {
+      k = i;
+      t2 = sum;
+      break;
+    }
+    const int pos = bq;
+    const int p = Lc[pos];
+    // next step's list (the other parity buffer, read by no one in this
+    // step): history through position i, the unchosen columns after it
+    for (int q = i - 1 + tid; q < N; q += nt) {
+      if (q >= 0) Ln[q] = (q == i) ? (short)p : ((q == pos) ? Lc[i] : Lc[q]);
+    }
+    // the previous step's diagonal: its column is read by no one any more
+    if (tid == 0 && pend_p >= 0) X[(size_t)pend_p * R + (i - 1)] = pend_a;
+    // (b) reflector of column p, rows i..R-1 (column p is not written in
+    // this step): H = I - beta v v^H, v = x - alpha e_i, alpha = -e |x|,
+    // v_i = e (|x_i| + |x|), beta = 1 / (|x| (|x| + |x_i|)), e = x_i / |x_i|
+    const E* v = X + (size_t)p * R;
+    S n2 = Q::zero();
+    for (int r = i + lane32; r < R; r += 32) n2 = Q::abs2_acc(v[r], n2);
+    for (int off = 16; off > 0; off >>= 1) n2 = Q::add(n2, Q::shfl(n2, off));
+    double s0x = 0.0, s0y = 0.0, sb = 0.0, sax = 0.0, say = 0.0;
+    if (lane32 == 0) {
+      const double nrm = sqrt(fmax(Q::tod(n2), 0.0));
+      const cx<double> x0 = Q::to(v[i]);
+      const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
+      const double ex = (a0 > 0.0) ? x0.x / a0 : 1.0, ey = (a0 > 0.0) ? x0.y / a0 : 0.0;
+      s0x = ex * (a0 + nrm);
+      s0y = ey * (a0 + nrm);
+      sb = (nrm > 0.0) ? 1.0 / (nrm * (nrm + a0)) : 0.0;
+      sax = -ex * nrm;
+      say = -ey * nrm;
+    }
+    s0x = __shfl_sync(0xffffffffu, s0x, 0);
+    s0y = __shfl_sync(0xffffffffu, s0y, 0);
+    sb = __shfl_sync(0xffffffffu, sb, 0);
+    if (tid == 0) {
+      pend_p = p;
+      pend_a = Q::from(mk<double>(sax, say));
+    }
+    const E v0 = Q::from(mk<double>(s0x, s0y));
+    const S beta = Q::fromd(sb);
+    // (c) apply H to the other unchosen columns (list positions i..N-1 but
+    // pos), refresh their partial norms (rows > i) in the other buffer
+    const int G = jacobi_group(R - i);
+    const int gl = tid & (G - 1), group = tid / G, ngroups = nt / G;
+    const int nrest = N - i - 1;
+    for (int tb = 0; tb < nrest; tb += ngroups) {
+      const int t = tb + group;
+      const bool act = t < nrest;
+      const int q = i + t + ((i + t >= pos) ? 1 : 0);
+      const int j = act ? Lc[q] : p;
+      E* cj = X + (size_t)j * R;
+      S wr = Q::zero(), wi = Q::zero();
+      if (act) {
+        for (int r = i + gl; r < R; r += G) Q::dotj(wr, wi, (r == i) ? v0 : v[r], cj[r]);
+      }
+      for (int off = G >> 1; off > 0; off >>= 1) {
+        wr = Q::add(wr, Q::shfl(wr, off));
+        wi = Q::add(wi, Q::shfl(wi, off));
+      }
+      float s2 = 0.f;
+      if (act) {
+        const S bx = Q::mul(beta, wr), by = Q::mul(beta, wi);
+        for (int r = i + gl; r < R; r += G) {
+          const E x = Q::sub_scaled(cj[r], (r == i) ? v0 : v[r], bx, by);
+          cj[r] = x;
+          if (r > i) s2 += Q::abs2f(x);
+        }
+      }
+      for (int off = G >> 1; off > 0; off >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, off, 32);
+      if (act && gl == 0) nxt[j] = s2;
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && pend_p >= 0) X[(size_t)pend_p * R + (k - 1)] = pend_a;
+  // a stop at step k leaves warps that may still be reading cn in that
+  // step's pivot search
+  __syncthreads();
+  // colstep from the final list (buffer k & 1), over cn's storage
+  const short* L = lists + (k & 1) * N;
+  int* colstep = reinterpret_cast<int*>(cn);
+  for (int q = tid; q < N; q += nt) colstep[L[q]] = (q < k) ? q : N;
+  __syncthreads();
+  *tail2 = t2;
+  return k;
+}
+
+// The split driver.  W (R x N, FP64, ld R) holds the oriented matrix and is
+// scratch afterwards; X (R x N elements of QA<T>::E) is the QR workspace; zs /
+// zs_bytes is spare shared memory for the Jacobi operand.  delta <= 0 selects
+// the default cut.  Returns the kept rank; *Wout (FP64, N x k, ld N, in X's
+// storage) holds V_A Sigma with norm / perm describing its columns as in
+// jacobi_finish.
+template <typename T>
+__device__ int qr_jacobi_truncate(cx<double>* W, int R, int N, typename QA<T>::E* X, unsigned char* zs,
+                                  size_t zs_bytes, double epsrel, float delta, double* norm, int* perm,
+                                  JacobiShared* sh, cx<double>** Wout) {
+  typedef QA<T> Q;
+  typedef typename Q::E E;
+  constexpr bool FF = Q::kFF;
+  const int tid = threadIdx.x;
+  const int nt = blockDim.x;
+  // scale by a power of two so that the largest entry is of order one (exact
+  // in FP64; keeps the double-float exponents in range)
+  double mx = 0.0;
+  for (int idx = tid; idx < R * N; idx += nt) mx = fmax(mx, fmax(fabs(W[idx].x), fabs(W[idx].y)));
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((tid & 31) == 0) sh->red[tid >> 5] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    double v = 0.0;
+    for (int w = 0; w < nt / 32; ++w) v = fmax(v, sh->red[w]);
+    sh->red[32] = (v > 0.0 && isfinite(v)) ? ldexp(1.0, ilogb(v)) : 1.0;
+  }
+  __syncthreads();
+  const double scale = sh->red[32];
+  const double inv = 1.0 / scale;
+  for (int idx = tid; idx < R * N; idx += nt) X[idx] = Q::from(cscale(W[idx], inv));
+  __syncthreads();
+  // QR bookkeeping in the (not yet used) norm / perm arrays: partial norms
+  // (2 N floats) then colstep (N ints) in norm[], column lists (2 N shorts)
+  // in perm[]
+  float* cn = reinterpret_cast<float*>(norm);
+  if (!(delta > 0.f)) delta = qr_default_delta(FF, epsrel);
+  float tail2;
+  const int k = qrcp_inplace<T>(X, R, N, delta, cn, reinterpret_cast<short*>(perm), &tail2);
+  const int* colstep = reinterpret_cast<const int*>(norm);
+  // Z = P R[0:k, :]^H: row q (original column q of A), column i
+  E* Z = ((size_t)N * k * sizeof(E) <= zs_bytes) ? reinterpret_cast<E*>(zs) : reinterpret_cast<E*>(W);
+  for (int idx = tid; idx < N * k; idx += nt) {
+    const int i = idx / N, q = idx - i * N;
+    Z[idx] = (colstep[q] >= i) ? Q::conj(X[(size_t)q * R + i]) : Q::zeroE();
+  }
+  __syncthreads();
+  int sw, sw64 = 0;
+  bool done;
+  cx<double>* O = reinterpret_cast<cx<double>*>(X);
+  if (FF) {
+    sw = jacobi_sweeps_ff(reinterpret_cast<cff*>(Z), N, k, N, sh);
+    done = sw < JACOBI_MAX_SWEEPS || sh->noise_converged;
+    for (int idx = tid; idx < N * k; idx += nt) O[idx] = cscale(Q::to(Z[idx]), scale);
+    __syncthreads();
+    // FP64 fallback: if the double-float sweeps did not settle, finish the
+    // (nearly orthogonal) matrix with FP64 sweeps; their count is reported
+    if (!done) {
+      sw64 = jacobi_sweeps<double>(O, N, k, N, nullptr, 0, sh);
+      done = true;
+    }
+  } else {
+    sw64 = jacobi_sweeps<double>(reinterpret_cast<cx<double>*>(Z), N, k, N, nullptr, 0, sh);
+    sw = 0;
+    for (int idx = tid; idx < N * k; idx += nt) O[idx] = cscale(Q::to(Z[idx]), scale);
+    __syncthreads();
+  }
+  if (tid == 0) sh->sweeps32 = sw;
+  const int kk = jacobi_finish<double>(O, N, k, N, epsrel, norm, perm, sh, sw64, (double)tail2 * scale * scale);
+  if (tid == 0) sh->sweeps = sw64;
+  __syncthreads();
+  *Wout = O;
+  return kk;
+}
+
+}  // namespace otb

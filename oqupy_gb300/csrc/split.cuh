@@ -2,14 +2,15 @@
 //
 // X is an m x n complex128 matrix read through an accessor X(row, col).  The
 // split orients itself so that the Jacobi columns are the smaller side, runs
-// the complex128 or double-float Jacobi (jacobi.cuh), and returns
+// the QR-preconditioned Jacobi (qr.cuh; plain Jacobi, jacobi.cuh, below 8
+// columns) in FP64 or double-float, and returns
 //   U  (m x kk, column-major, in Tg)      left singular vectors,
 //   C  (kk x n, row-major, in Cg)         S V^H (the carry),
 // with kk the kept rank of the relative tail rule.  The caller copies U to its
 // destination after the call (U never aliases X, so X may be the destination).
 #pragma once
 
-#include "jacobi.cuh"
+#include "qr.cuh"
 
 namespace otb {
 
@@ -34,7 +35,7 @@ struct SplitShared {
 
 // Returns kk (>= 1); on failure sets *status (nonzero) and returns 0.
 template <bool MIXED, class Acc>
-__device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap, SplitBufs& b,
+__device__ int split_generic(const Acc& X, int m, int n, double epsrel, float qr_delta, int cap, SplitBufs& b,
                              SplitShared& sh, int* status, int* sweeps64, int* sweepsff,
                              double* flops) {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -48,8 +49,10 @@ __device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap,
     used += bytes;
     return p;
   };
+  // QR / double-float workspace (16 bytes per element in both forms)
+  const bool flip = N >= 8;
   cff* Wff = nullptr;
-  if (MIXED) {
+  if (MIXED || flip) {
     Wff = (cff*)take((size_t)R * N * sizeof(cff));
     if (!Wff) Wff = b.Wffg;
   }
@@ -61,15 +64,21 @@ __device__ int split_generic(const Acc& X, int m, int n, double epsrel, int cap,
     W[idx] = trans ? cconj(X(c, r)) : X(r, c);
   }
   __syncthreads();
-  // the QR-preconditioned mixed driver returns X^H U (N x kk, ld N) instead of
-  // X V (R x N, ld R): the same two branches below, swapped
-  const bool flip = MIXED && N >= 8;
+  // the QR-preconditioned driver (qr.cuh) returns X^H U (N x kk, ld N)
+  // instead of X V (R x N, ld R): the same two branches below, swapped
   zc* Wr = W;
   const size_t spare = (size_t)b.smem_bytes > used ? (size_t)b.smem_bytes - used : 0;
-  const int kk = flip ? jacobi_truncate_mixed_qr(W, R, N, Wff, b.smem + used, spare, epsrel, sh.norm,
-                                                 sh.perm, &sh.jsh, &Wr)
-                 : MIXED ? jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh)
-                         : jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
+  int kk;
+  if (flip && MIXED)
+    kk = qr_jacobi_truncate<ff>(W, R, N, Wff, b.smem + used, spare, epsrel, qr_delta, sh.norm, sh.perm,
+                                &sh.jsh, &Wr);
+  else if (flip)
+    kk = qr_jacobi_truncate<double>(W, R, N, reinterpret_cast<zc*>(Wff), b.smem + used, spare, epsrel,
+                                    qr_delta, sh.norm, sh.perm, &sh.jsh, &Wr);
+  else if (MIXED)
+    kk = jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh);
+  else
+    kk = jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
   W = Wr;
   *sweeps64 += sh.jsh.sweeps;  // mixed form: FP64 fallback sweeps only
   *sweepsff += MIXED ? sh.jsh.sweeps32 : 0;

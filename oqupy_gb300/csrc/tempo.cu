@@ -31,19 +31,17 @@
 #include <math.h>
 
 #include <cmath>
-#include <mutex>
 
 #include "../../include/oqupy_gb300.h"
 #include "capi_util.h"
 
 #include "engine.h"
-#include "jacobi.cuh"
+#include "qr.cuh"
 
 namespace otb {
 
 constexpr int TEMPO_THREADS = 256;
-constexpr int NMAX = 1152;   // max columns of a split (D * cap <= 9 * 128)
-constexpr int VMAX = 128;    // max bond dimension held by the read-out vector (chi_cap <= 128)
+constexpr int NMAX = 1152;   // max columns of a split (D * cap <= 1152)
 
 typedef cx<double> zc;
 
@@ -66,7 +64,6 @@ struct SharedStep {
   JacobiShared jsh;
   double norm[NMAX];
   int perm[NMAX];
-  zc v[2][VMAX];
   int inst;
 };
 
@@ -80,7 +77,7 @@ struct SharedStep {
 constexpr int QR_MIN_COLS = 8;
 
 template <bool MIXED>
-__device__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel,
+__device__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel, float qr_delta,
                      Bufs& b, SharedStep& sh, zc** Wout, bool* flip) {
   const int tid = threadIdx.x, nt = blockDim.x;
   size_t used = 0;
@@ -91,8 +88,10 @@ __device__ int split(const zc* src, int lds, bool src_trans, int R, int N, doubl
     used += bytes;
     return p;
   };
+  // QR workspace (16 bytes per element in both forms: cff or complex128)
+  const bool qr = N >= QR_MIN_COLS;
   cff* Wff = nullptr;
-  if (MIXED) {
+  if (MIXED || qr) {
     Wff = (cff*)take((size_t)R * N * sizeof(cff));
     if (!Wff) Wff = b.Wffg;
   }
@@ -105,11 +104,14 @@ __device__ int split(const zc* src, int lds, bool src_trans, int R, int N, doubl
   __syncthreads();
   int kk;
   *flip = false;
-  if (MIXED && N >= QR_MIN_COLS) {
+  if (qr) {
     *flip = true;
     const size_t spare = (size_t)b.smem_bytes > used ? (size_t)b.smem_bytes - used : 0;
-    return jacobi_truncate_mixed_qr(W, R, N, Wff, b.smem + used, spare, epsrel, sh.norm, sh.perm,
+    if (MIXED)
+      return qr_jacobi_truncate<ff>(W, R, N, Wff, b.smem + used, spare, epsrel, qr_delta, sh.norm, sh.perm,
                                     &sh.jsh, Wout);
+    return qr_jacobi_truncate<double>(W, R, N, reinterpret_cast<zc*>(Wff), b.smem + used, spare, epsrel,
+                                      qr_delta, sh.norm, sh.perm, &sh.jsh, Wout);
   }
   if (MIXED) {
     kk = jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh);
@@ -169,13 +171,13 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     for (int c = tid; c < r0; c += nt) {
       zc acc = mk<double>(0, 0);
       for (int a = 0; a < D; ++a) acc = acc + A0[a * r0 + c];
-      sh.v[0][c] = acc;
+      b.Cg[c] = acc;
     }
     __syncthreads();
     for (int idx = tid; idx < D * r1; idx += nt) {
       const int a = idx / r1, rr = idx - a * r1;
       zc acc = mk<double>(0, 0);
-      for (int c = 0; c < r0; ++c) cfma(acc, sh.v[0][c], A1[((long long)c * D + a) * r1 + rr]);
+      for (int c = 0; c < r0; ++c) cfma(acc, b.Cg[c], A1[((long long)c * D + a) * r1 + rr]);
       b.Tg[idx] = acc;
     }
     __syncthreads();
@@ -248,8 +250,8 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     const bool trans = n > m;
     zc* W;
     bool flip;
-    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, b, sh, &W, &flip)
-                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, b, sh, &W, &flip);
+    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
+                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
     {
       const double R = trans ? n : m, N = trans ? m : n;
       flops += 8.0 * m * n * ccd + 4.0 * (6.0 * R * N * N + 20.0 * N * N * N);
@@ -356,8 +358,8 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       const bool trans = n > m;
       zc* W;
       bool flip;
-      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, b, sh, &W, &flip)
-                           : split<MIXED>(A, m, false, m, n, I.epsrel, b, sh, &W, &flip);
+      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
+                           : split<MIXED>(A, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
       {
         const double R = trans ? n : m, N = trans ? m : n;
         flops += 4.0 * (6.0 * R * N * N + 20.0 * N * N * N) + 8.0 * DIMS(k - 1).x * D * (double)kk * n;
@@ -504,7 +506,9 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
   // 6. read-out: v <- sum_{c,a} v[c] A[c][a][r] over all sites, state = P2 v
   {
     int cur = 0;
-    if (tid == 0) sh.v[0][0] = mk<double>(1, 0);
+    // the two read-out vectors live in the carry buffer (dead after the sweep)
+    zc* const vv[2] = {b.Cg, b.Cg + cap};
+    if (tid == 0) vv[0][0] = mk<double>(1, 0);
     __syncthreads();
     int maxb = 1;
     for (int k = 0; k < K; ++k) {
@@ -517,16 +521,16 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
         for (int c = 0; c < l; ++c) {
           zc part = mk<double>(0, 0);
           for (int a = 0; a < D; ++a) part = part + A[((long long)c * D + a) * r + rr];
-          cfma(acc, sh.v[cur][c], part);
+          cfma(acc, vv[cur][c], part);
         }
-        sh.v[cur ^ 1][rr] = acc;
+        vv[cur ^ 1][rr] = acc;
       }
       __syncthreads();
       cur ^= 1;
     }
     if (tid < D) {
       zc acc = mk<double>(0, 0);
-      for (int c = 0; c < D; ++c) cfma(acc, P2[tid * D + c], sh.v[cur][c]);
+      for (int c = 0; c < D; ++c) cfma(acc, P2[tid * D + c], vv[cur][c]);
       b.out[I.out_base + (long long)((step - I.out_origin) % I.out_cap) * D + tid] = acc;
     }
     if (tid == 0) {
@@ -625,7 +629,7 @@ static __device__ __align__(256) unsigned char g_tempo_static_scratch[STATIC_SCR
 
 template <bool MIXED>
 __global__ void __launch_bounds__(TEMPO_THREADS)
-    tempo_static_kernel(TempoLaunch L, InstDev I, const double* rho0, int nsteps) {
+    tempo_static_kernel(TempoLaunch L, InstDev I, const double* rho0, int nsteps, int* status_out) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ SharedStep sh;
   Bufs b;
@@ -656,23 +660,22 @@ __global__ void __launch_bounds__(TEMPO_THREADS)
     __syncthreads();
   }
   I.out_origin = sh.st.step + 1;  // states of this call fill out[0 .. nsteps)
+  const int first = sh.st.step;
   __syncthreads();
   for (int s = 0; s < nsteps; ++s) {
     tempo_step<MIXED>(L, I, 0, b, sh);
     __syncthreads();
     if (sh.st.status != ST_OK) break;
   }
+  if (tid == 0) {
+    status_out[0] = sh.st.status;
+    status_out[1] = sh.st.step - first;
+    status_out[2] = sh.st.step;
+    status_out[3] = sh.st.max_bond;
+  }
 }
 
 }  // namespace otb
-
-namespace {
-
-std::mutex g_static_mutex;
-void* g_static_addr[64];
-bool g_static_ready[64];
-
-}  // namespace
 
 extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, int32_t nsteps,
                                                void* stream) {
@@ -690,26 +693,18 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
     return set_error(OTB_ERR_INVALID_ARG, "epsrel must be positive and finite");
   if (io->precision != 0 && io->precision != 1)
     return set_error(OTB_ERR_INVALID_ARG, "precision must be 0 (complex128) or 1 (mixed)");
-  if (!io->influences || !io->props || !io->rho0 || !io->mps || !io->states_out)
+  if (!io->influences || !io->props || !io->rho0 || !io->mps || !io->states_out || !io->status_out)
     return set_error(OTB_ERR_INVALID_ARG, "null device buffer");
   if (nsteps < 1) return set_error(OTB_ERR_INVALID_ARG, "nsteps must be >= 1");
   if (io->mps_bytes < (int64_t)OTB_TEMPO_STATIC_MPS_BYTES(io->hs_dim, io->dkmax, io->chi_cap))
     return set_error(OTB_ERR_INVALID_ARG, "mps buffer smaller than OTB_TEMPO_STATIC_MPS_BYTES");
-  int dev = 0;
-  if (!check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return OTB_ERR_CUDA;
-  if (dev < 0 || dev >= 64) return set_error(OTB_ERR_INVALID_ARG, "device index out of range");
-  {
-    // once per device, with that device current: the scratch array's device
-    // address (the symbol name is only a host-side stand-in)
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_ready[dev]) {
-      void* p = nullptr;
-      if (!check_cuda(cudaGetSymbolAddress(&p, g_tempo_static_scratch), "cudaGetSymbolAddress"))
-        return OTB_ERR_CUDA;
-      g_static_addr[dev] = p;
-      g_static_ready[dev] = true;
-    }
-  }
+  // the scratch array's device address for the current device and context
+  // (the symbol name is only a host-side stand-in); looked up on every call,
+  // so a device reset or another current context is followed.  It allocates
+  // nothing; the first call on a device loads the module there.
+  void* scratch = nullptr;
+  if (!check_cuda(cudaGetSymbolAddress(&scratch, g_tempo_static_scratch), "cudaGetSymbolAddress"))
+    return OTB_ERR_CUDA;
   const int nslots = io->dkmax + 2;
   unsigned char* mps = (unsigned char*)io->mps;
   InstDev I;
@@ -718,6 +713,7 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
   I.cap = io->chi_cap;
   I.nslots = nslots;
   I.epsrel = io->epsrel;
+  I.qr_delta = 0.f;
   I.site_base = 0;
   I.dims_base = 0;
   I.infl_base = 0;
@@ -736,7 +732,7 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
   L.infl = io->influences;
   L.props = io->props;
   L.out = io->states_out;
-  L.work = g_static_addr[dev];
+  L.work = scratch;
   L.work_stride = 0;
   L.wcap = (long long)(io->chi_cap * D) * (io->chi_cap * D);
   L.queue = nullptr;
@@ -748,10 +744,10 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
   cudaError_t e;
   if (io->precision == 0) {
     e = cudaFuncSetAttribute(tempo_static_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) tempo_static_kernel<false><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps);
+    if (e == cudaSuccess) tempo_static_kernel<false><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
   } else {
     e = cudaFuncSetAttribute(tempo_static_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) tempo_static_kernel<true><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps);
+    if (e == cudaSuccess) tempo_static_kernel<true><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
   }
   if (e == cudaSuccess) e = cudaGetLastError();
   if (!check_cuda(e, "otb_tempo_advance_static launch")) return OTB_ERR_CUDA;

@@ -9,13 +9,18 @@ class otherwise, so existing code selects the GPU path through its existing
 configuration.  The factory dispatches before the reference constructor runs,
 so the reference never sees the unknown backend name.
 
+``PtTempo.get_process_tensor`` (oqupy/pt_tempo.py:280-306) returns, for a
+GPU build, a ``DeviceProcessTensor`` (``device_pt.py``): a
+``BaseProcessTensor`` whose tensors stay in device memory.
+
 ``compute_dynamics`` has no configuration argument
 (oqupy/system_dynamics.py:41-53): the wrapper routes a call to the GPU sweep
-when its single process tensor was built by the GPU backend (it carries a
-device twin), there is no control and ``record_all`` is set, and otherwise
-calls the reference function.  Both ``oqupy.system_dynamics.compute_dynamics``
-and ``oqupy.compute_dynamics`` (bound at import, oqupy/__init__.py:104) are
-rebound.
+when its single process tensor is a ``DeviceProcessTensor``, there is no
+control and ``record_all`` is set, and otherwise calls the reference
+function (a ``DeviceProcessTensor`` that the reference must handle is
+first copied to a host ``SimpleProcessTensor``).  Both
+``oqupy.system_dynamics.compute_dynamics`` and ``oqupy.compute_dynamics``
+(bound at import, oqupy/__init__.py:104) are rebound.
 """
 
 from typing import Any, Dict, Optional
@@ -68,6 +73,22 @@ def install(oqupy_module: Any = None) -> None:
         pt_tempo_backend.reference_class = ref_pt
         pt_mod.PtTempoBackend = pt_tempo_backend
 
+    if "get_process_tensor" not in _installed:
+        ref_get = pt_mod.PtTempo.get_process_tensor
+        _installed["get_process_tensor"] = ref_get
+        ptm = importlib.import_module(oqupy_module.__name__ + ".process_tensor")
+
+        def get_process_tensor(self, progress_type=None):
+            be = self._backend_instance
+            if not isinstance(be, GpuPtTempoBackend):
+                return ref_get(self, progress_type=progress_type)
+            if be.step is None or be.step < be.num_steps:
+                self.compute(progress_type=progress_type)
+            return be.device_process_tensor(ptm.BaseProcessTensor)
+
+        get_process_tensor.reference_function = ref_get
+        pt_mod.PtTempo.get_process_tensor = get_process_tensor
+
     sd_mod = importlib.import_module(oqupy_module.__name__ + ".system_dynamics")
     if "compute_dynamics" not in _installed:
         ref_cd = sd_mod.compute_dynamics
@@ -75,6 +96,12 @@ def install(oqupy_module: Any = None) -> None:
         _installed["compute_dynamics_pkg"] = getattr(oqupy_module, "compute_dynamics", None)
         sys_mod = importlib.import_module(oqupy_module.__name__ + ".system")
         dyn_mod = importlib.import_module(oqupy_module.__name__ + ".dynamics")
+        ptm = importlib.import_module(oqupy_module.__name__ + ".process_tensor")
+        from .device_pt import device_process_tensor_class
+        dev_cls = device_process_tensor_class(ptm.BaseProcessTensor)
+
+        def host_copy(pt):
+            return pt.to_host(ptm.SimpleProcessTensor) if isinstance(pt, dev_cls) else pt
 
         def compute_dynamics(system, initial_state=None, dt=None, num_steps=None,
                              start_time=0.0, process_tensor=None, control=None,
@@ -90,9 +117,12 @@ def install(oqupy_module: Any = None) -> None:
                 kwargs["liouvillian_epsrel"] = liouvillian_epsrel
             pts = process_tensor if isinstance(process_tensor, list) else \
                 ([] if process_tensor is None else [process_tensor])
-            gpu = (len(pts) == 1 and hasattr(pts[0], "_gb300") and control is None
+            gpu = (len(pts) == 1 and isinstance(pts[0], dev_cls) and control is None
                    and record_all and type(system) is sys_mod.System)
             if not gpu:
+                if any(isinstance(p, dev_cls) for p in pts):
+                    hosts = [host_copy(p) for p in pts]
+                    kwargs["process_tensor"] = hosts if isinstance(process_tensor, list) else hosts[0]
                 return ref_cd(system, **kwargs)
             parsed = sd_mod._compute_dynamics_input_parse(
                 False, system, initial_state, dt, num_steps, start_time,
@@ -123,9 +153,11 @@ def uninstall(oqupy_module: Any = None) -> None:
     tempo_mod = importlib.import_module(oqupy_module.__name__ + ".tempo")
     if "TempoBackend" in _installed:
         tempo_mod.TempoBackend = _installed.pop("TempoBackend")
+    pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
     if "PtTempoBackend" in _installed:
-        pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
         pt_mod.PtTempoBackend = _installed.pop("PtTempoBackend")
+    if "get_process_tensor" in _installed:
+        pt_mod.PtTempo.get_process_tensor = _installed.pop("get_process_tensor")
     if "compute_dynamics" in _installed:
         sd_mod = importlib.import_module(oqupy_module.__name__ + ".system_dynamics")
         sd_mod.compute_dynamics = _installed.pop("compute_dynamics")

@@ -29,7 +29,7 @@ class PtBatch:
     """
 
     def __init__(self, instances: Sequence[Dict], precision: str = "complex128",
-                 chi_cap: int = DEFAULT_CHI_CAP, grid: int = 0):
+                 chi_cap: int = DEFAULT_CHI_CAP, grid: int = 0, qr_cut: float = 0.0):
         L = nat.lib()
         if precision not in nat.PRECISION:
             raise ValueError(f"precision must be one of {list(nat.PRECISION)}")
@@ -62,7 +62,7 @@ class PtBatch:
             else:
                 arr[i].neg_influences = None
             self.meta.append(dict(d=d, D=D, num_steps=num_steps))
-        cfg = nat.PtConfig(nat.PRECISION[precision], int(chi_cap), int(grid))
+        cfg = nat.PtConfig(nat.PRECISION[precision], int(chi_cap), int(grid), float(qr_cut))
         self.chi_cap = int(chi_cap)
         h = ctypes.c_void_p()
         nat.check(L.otb_pt_create(ctypes.byref(cfg), self.n, arr, ctypes.byref(h)))
@@ -153,10 +153,15 @@ class GpuPtTempoBackend:
     """Drop-in for ``oqupy.backends.pt_tempo_backend.PtTempoBackend``
     (pt_tempo_backend.py:56-316): same constructor, ``step``/``num_steps``,
     ``initialize()``, ``compute_step() -> bool``, ``get_mpo_tensor(step)``,
-    ``update_process_tensor()``.  The process tensor handed in receives host
-    copies of the tensors (and computes its caps as in the reference); it also
-    gets a device twin (attribute ``_gb300``) that ``compute_dynamics`` uses
-    once ``oqupy_gb300.install`` has run."""
+    ``update_process_tensor()`` (host copies into the process tensor handed
+    in, caps computed as in the reference).  ``device_process_tensor()``
+    returns the build as a ``DeviceProcessTensor`` (``device_pt.py``) whose
+    tensors stay on the GPU; ``PtTempo.get_process_tensor`` returns that once
+    ``oqupy_gb300.install`` has run.
+
+    ``config`` keys used: ``precision`` ("complex128" | "mixed"),
+    ``chi_cap`` (initial bond capacity; a build whose bonds outgrow it is
+    rebuilt with twice the capacity, up to 1152 / D), ``qr_cut``."""
 
     def __init__(self, dimension, influence: Callable[[int], np.ndarray], process_tensor,
                  sum_north, sum_west, num_steps, dkmax, epsrel, config: Dict,
@@ -199,17 +204,40 @@ class GpuPtTempoBackend:
                     neg[s] = m
                 else:
                     neg[s] = infl[-1]
-        inst = dict(hs_dim=self._d, num_steps=self._num_steps, dkmax=self._dkmax,
-                    epsrel=self._epsrel, influences=infl, neg_influences=neg)
-        self._batch = PtBatch([inst], precision=self._config.get("precision", "complex128"),
-                              chi_cap=int(self._config.get("chi_cap", DEFAULT_CHI_CAP)),
-                              grid=1)
+        self._inst = dict(hs_dim=self._d, num_steps=self._num_steps, dkmax=self._dkmax,
+                          epsrel=self._epsrel, influences=infl, neg_influences=neg)
+        self._cap = int(self._config.get("chi_cap", DEFAULT_CHI_CAP))
+        self._new_batch()
         self._batch.advance(0)
         self._step = 1
+        self._check_grow()
+
+    def _new_batch(self):
+        if self._batch is not None:
+            self._batch.close()
+        self._batch = PtBatch([self._inst], precision=self._config.get("precision", "complex128"),
+                              chi_cap=self._cap, grid=1,
+                              qr_cut=float(self._config.get("qr_cut", 0.0)))
+
+    def _check_grow(self):
+        """A bond beyond the capacity stops the build on the device: rebuild
+        with twice the capacity (up to 1152 / D) and replay the steps done so
+        far (the build is deterministic, so the replay repeats them)."""
+        while True:
+            st = self._batch.info(0)["status"]
+            if st == 0:
+                return
+            cap_max = nat.MAX_COLUMNS // (self._d * self._d)
+            if st != nat.OTB_ERR_CHI_OVERFLOW or self._cap >= cap_max:
+                raise nat.DeviceError(st, f"PT-TEMPO step {self._step}")
+            self._cap = min(2 * self._cap, cap_max)
+            self._new_batch()
+            self._batch.advance(self._step - 1)      # initialise, then replay
 
     def compute_step(self) -> bool:
         self._batch.advance(1)
         self._step += 1
+        self._check_grow()
         return self._step < self._num_steps
 
     def get_mpo_tensor(self, step: int) -> np.ndarray:
@@ -220,19 +248,32 @@ class GpuPtTempoBackend:
         for step in reversed(range(self._num_steps)):
             self._process_tensor.set_mpo_tensor(step, self.get_mpo_tensor(step))
         self._process_tensor.compute_caps()
-        self._process_tensor._gb300 = (self._batch, 0)
+
+    def device_process_tensor(self, base_cls=None):
+        """The build as a ``DeviceProcessTensor`` with the dt, transforms,
+        name and description of the process tensor handed in; ``base_cls``
+        is the reference's ``BaseProcessTensor`` (default: the base class of
+        that process tensor's class hierarchy)."""
+        from .device_pt import device_process_tensor_class
+        self._batch.check_status()
+        pt = self._process_tensor
+        if base_cls is None:
+            base_cls = next(c for c in type(pt).__mro__ if c.__name__ == "BaseProcessTensor")
+        cls = device_process_tensor_class(base_cls)
+        return cls(self._batch, 0, pt.hilbert_space_dimension, pt.dt, pt.transform_in,
+                   pt.transform_out, getattr(pt, "name", None), getattr(pt, "description", None))
 
 
 def device_compute_dynamics(process_tensor, propagator_pairs, initial_states,
                             num_steps: Optional[int] = None) -> np.ndarray:
-    """GPU sweep for several systems on a process tensor built by
-    ``GpuPtTempoBackend`` (or ``(PtBatch, index)``).  ``propagator_pairs``:
-    list of ``(P1, P2)``; returns ``[num_steps+1, H, D]`` states."""
+    """GPU sweep for several systems on a ``DeviceProcessTensor`` (or a
+    ``(PtBatch, index)`` pair).  ``propagator_pairs``: list of ``(P1, P2)``;
+    returns ``[num_steps+1, H, D]`` states."""
     if isinstance(process_tensor, tuple):
         batch, idx = process_tensor
         tin = tout = None
     else:
-        batch, idx = process_tensor._gb300
+        batch, idx = process_tensor.device
         tin, tout = process_tensor.transform_in, process_tensor.transform_out
     p1 = np.array([p[0] for p in propagator_pairs])
     p2 = np.array([p[1] for p in propagator_pairs])

@@ -70,11 +70,13 @@ class TempoBatch:
     precision: ``"complex128"`` or ``"mixed"``.
     chi_cap: bond-dimension capacity of every site slot.
     out_cap: number of recent states kept per instance on the device.
+    qr_cut: relative cut of the rank-revealing QR in every bond split
+        (0 = the precision form's default; ``otb_tempo_config.qr_cut``).
     """
 
     def __init__(self, instances: Sequence[Dict], precision: str = "complex128",
                  chi_cap: int = DEFAULT_CHI_CAP, out_cap: int = 2, grid: int = 0,
-                 max_sites: int = 0, block: int = 0, smem_kb: int = 0):
+                 max_sites: int = 0, block: int = 0, smem_kb: int = 0, qr_cut: float = 0.0):
         L = nat.lib()
         if precision not in nat.PRECISION:
             raise ValueError(f"precision must be one of {list(nat.PRECISION)}")
@@ -106,7 +108,8 @@ class TempoBatch:
             arr[i].max_sites = int(max_sites)
             self.D.append(D)
         cfg = nat.TempoConfig(nat.PRECISION[precision], int(chi_cap),
-                              int(out_cap), int(grid), int(block), int(smem_kb))
+                              int(out_cap), int(grid), int(block), int(smem_kb),
+                              float(qr_cut))
         self.out_cap = int(out_cap)
         self.chi_cap = int(chi_cap)
         h = ctypes.c_void_p()
@@ -221,9 +224,13 @@ class GpuTempoBackend:
     (tempo_backend.py:577-626): same constructor, ``step`` property,
     ``initialize() -> (0, state)`` and ``compute_step() -> (step, state)``.
 
-    ``config`` keys used: ``precision`` ("complex128" | "mixed"), ``chi_cap``.
-    Degeneracy maps (``unique=True``) are not supported by the GPU engine;
-    ``oqupy_gb300.install`` routes such runs to the reference backend.
+    ``config`` keys used: ``precision`` ("complex128" | "mixed"), ``chi_cap``
+    (initial bond capacity; a step whose bonds outgrow it is redone with
+    twice the capacity, up to 1152 / D, after replaying the earlier steps on
+    a fresh handle -- the engine is deterministic, so the replay repeats
+    them), ``qr_cut``.  Degeneracy maps (``unique=True``) are not supported by
+    the GPU engine; ``oqupy_gb300.install`` routes such runs to the reference
+    backend.
     """
 
     def __init__(self, initial_state, influence: Callable[[int], np.ndarray],
@@ -245,10 +252,16 @@ class GpuTempoBackend:
         self._batch: Optional[TempoBatch] = None
         self._last_props = None
         self._ninfl = 0
+        self._slots = 16
 
     @property
     def step(self):
         return self._step
+
+    @property
+    def chi_cap(self) -> int:
+        """Current bond capacity of the device handle."""
+        return self._cap
 
     def initialize(self):
         D = self._initial_state.size
@@ -257,21 +270,33 @@ class GpuTempoBackend:
         infl = np.array([self._influence(dk) for dk in range(n)],
                         dtype=np.complex128)
         p1, p2 = self._propagators(0)
-        self._last_props = (np.array(p1), np.array(p2))
-        inst = dict(hs_dim=d, dkmax=self._dkmax, epsrel=self._epsrel,
-                    influences=infl, prop1=p1, prop2=p2,
-                    rho0=self._initial_state, unitary=self._unitary)
-        self._batch = TempoBatch(
-            [inst], precision=self._config.get("precision", "complex128"),
-            chi_cap=int(self._config.get("chi_cap", DEFAULT_CHI_CAP)),
-            out_cap=4, grid=1, max_sites=16 if self._dkmax is None else 0)
-        self._ninfl = n
+        self._inst = dict(hs_dim=d, dkmax=self._dkmax, epsrel=self._epsrel,
+                          influences=infl, prop1=np.array(p1), prop2=np.array(p2),
+                          rho0=self._initial_state, unitary=self._unitary)
+        self._cap = max(int(self._config.get("chi_cap", DEFAULT_CHI_CAP)), D)
+        self._cap_max = nat.MAX_COLUMNS // D
+        self._new_batch()
         self._step = 0
         return self._step, copy(self._initial_state)
 
-    def compute_step(self):
+    def _new_batch(self):
+        if self._batch is not None:
+            self._batch.close()
+        inst = self._inst
+        self._batch = TempoBatch(
+            [inst], precision=self._config.get("precision", "complex128"),
+            chi_cap=self._cap, out_cap=4, grid=1,
+            max_sites=16 if self._dkmax is None else 0,
+            qr_cut=float(self._config.get("qr_cut", 0.0)))
+        self._ninfl = len(inst["influences"])
+        self._last_props = (inst["prop1"], inst["prop2"])
+        self._slots = 16
+
+    def _advance(self, step: int) -> int:
+        """Inputs of ``step`` (propagators, influences of a growing memory,
+        the first-site influence past dkmax), one engine step; returns the
+        instance's status."""
         b = self._batch
-        step = self._step + 1
         p1, p2 = self._propagators(step - 1)
         if not (np.array_equal(p1, self._last_props[0])
                 and np.array_equal(p2, self._last_props[1])):
@@ -283,20 +308,28 @@ class GpuTempoBackend:
                 b.set_influence(0, self._ninfl, self._influence(self._ninfl))
                 self._ninfl += 1
             need = step + 2
-            if b.info(0)["nsites"] + 2 > getattr(self, "_slots", 16):
-                self._slots = max(2 * getattr(self, "_slots", 16), need)
+            if b.info(0)["nsites"] + 2 > self._slots:
+                self._slots = max(2 * self._slots, need)
                 b.reserve_sites(self._slots)
         elif step > self._dkmax:
             neg = self._influence(self._dkmax - step)
             if neg is not None:
                 b.set_first_influence(0, neg)
         b.advance(1)
-        inf = b.info(0)
-        if inf["status"] != 0:
-            raise nat.DeviceError(inf["status"], f"TEMPO step {step}")
-        state = b.instance_states(0, step, 1)[0]
+        return b.info(0)["status"]
+
+    def compute_step(self):
+        step = self._step + 1
+        st = self._advance(step)
+        while st == nat.OTB_ERR_CHI_OVERFLOW and self._cap < self._cap_max:
+            self._cap = min(2 * self._cap, self._cap_max)
+            self._new_batch()
+            for s in range(1, step + 1):
+                st = self._advance(s)
+                if st != 0:
+                    break
+        if st != 0:
+            raise nat.DeviceError(st, f"TEMPO step {step}")
+        state = self._batch.instance_states(0, step, 1)[0]
         self._step = step
         return self._step, state
-
-    def bond_dimensions(self) -> List[int]:
-        return self._batch.bond_dims(0)

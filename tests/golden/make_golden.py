@@ -3,7 +3,7 @@
 Run from the repository root, in a container where the reference sources are
 present (it cannot run on a machine without them):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <OQuPy source tree> [case ...]
 
 The reference imports the third-party ``tensornetwork`` package, which is not
 installed here; ``oracle/tnshim`` provides a from-scratch stand-in for the few
@@ -251,7 +251,9 @@ def run_case(oqupy, name, c):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py <OQuPy source tree> [case ...]")
+    ref_root = sys.argv[1]
     oqupy = _import_reference(ref_root)
     only = sys.argv[2:] if len(sys.argv) > 2 else None
     for name, c in cases(oqupy):

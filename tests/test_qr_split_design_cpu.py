@@ -1,48 +1,65 @@
-"""The mixed form's QR-preconditioned bond split, restated in numpy (exact
-SVD in place of the double-float Jacobi) and checked against the plain
-truncated SVD: pivoted Householder QR stopped once the trailing block falls
-below min(1e-3 epsrel, 1e-9) |R_00|, the SVD of the k rows of R, the
-dropped block's squared norm added to the tail sums.  The kept rank must be
-the full SVD's and the reconstruction error its truncation error."""
+"""The QR-preconditioned bond split of both precision forms, restated in
+numpy (exact SVD in place of the one-sided Jacobi) and checked against the
+plain truncated SVD: pivoted Householder QR without column exchanges,
+stopped once the remaining block falls below delta |R_00| (mixed form:
+min(1e-3 epsrel, 1e-9); complex128 form: 1e-14), the SVD of the k rows of
+R, the dropped block's squared norm added to the tail sums.  The kept rank
+must be the full SVD's and the reconstruction error its truncation error."""
 import numpy as np
 
 from oracle import tempo_oracle as to
 
 
-def qr_truncated_split(A, epsrel):
-    """A (R x N, R >= N) -> (U, S V^H, kept) as the mixed-form kernel forms
-    them (U = A W / s^2 with W = A^H U S)."""
+def qr_truncated_split(A, epsrel, delta=None):
+    """A (R x N, R >= N) -> (U, S V^H, kept, k) as the kernel forms them
+    (oqupy_gb300/csrc/qr.cuh): pivoted Householder QR without column
+    exchanges (colstep[j] = step at which column j was chosen, N = never),
+    partial norms double-buffered by step parity, the diagonal stored one
+    step late, Z[q, i] = conj(R[i, q]) for colstep[q] >= i, then the SVD of
+    Z (exact here, one-sided Jacobi on the GPU); U = A W / s^2 with
+    W = A^H U S."""
     X = np.array(A, dtype=np.complex128)
     R, N = X.shape
-    piv = np.arange(N)
-    cn = np.sum(np.abs(X) ** 2, axis=0)
-    delta = min(1e-3 * epsrel, 1e-9)
+    if delta is None:
+        delta = min(1e-3 * epsrel, 1e-9)
+    colstep = np.full(N, N)
+    cn = [np.sum(np.abs(X) ** 2, axis=0), np.zeros(N)]
     k, tail2, r00 = N, 0.0, None
+    pend = None
     for i in range(N):
-        p = i + int(np.argmax(cn[i:]))
-        tot = float(cn[i:].sum())
+        cur, nxt = cn[i & 1], cn[(i + 1) & 1]
+        avail = np.flatnonzero(colstep >= i)
+        p = int(avail[np.argmax(cur[avail])])          # lowest index on ties
+        tot = float(cur[avail].sum())
         if i == 0:
-            r00 = float(cn[p])
+            r00 = float(cur[p])
         elif tot < delta * delta * r00:
             k, tail2 = i, tot
             break
-        X[:, [i, p]] = X[:, [p, i]]
-        cn[[i, p]] = cn[[p, i]]
-        piv[[i, p]] = piv[[p, i]]
-        x = X[i:, i]
+        colstep[p] = i
+        if pend is not None:                            # previous diagonal
+            X[i - 1, pend[0]] = pend[1]
+        x = X[i:, p]
         nrm = np.linalg.norm(x)
         a0 = abs(x[0])
         e = x[0] / a0 if a0 > 0 else 1.0
         v = x.copy()
         v[0] = e * (a0 + nrm)
         beta = 1.0 / (nrm * (nrm + a0)) if nrm > 0 else 0.0
-        X[i:, i + 1:] -= beta * np.outer(v, v.conj() @ X[i:, i + 1:])
-        X[i, i] = -e * nrm
-        X[i + 1:, i] = 0
-        cn[i + 1:] = np.sum(np.abs(X[i + 1:, i + 1:]) ** 2, axis=0)
-    Rk = np.triu(X[:k, :])
+        pend = (p, -e * nrm)
+        for j in range(N):
+            if j == p or colstep[j] < i:
+                continue
+            w = np.vdot(v, X[i:, j])
+            X[i:, j] -= beta * v * w
+            nxt[j] = np.sum(np.abs(X[i + 1:, j]) ** 2)
+    if pend is not None:
+        X[k - 1, pend[0]] = pend[1]
     Z = np.zeros((N, k), dtype=np.complex128)
-    Z[piv, :] = Rk.conj().T                          # Z = P R_k^H
+    for i in range(k):
+        for q in range(N):
+            if colstep[q] >= i:
+                Z[q, i] = np.conj(X[i, q])
     u, s, vh = np.linalg.svd(Z, full_matrices=False)
     W = u * s                                        # Z V: orthogonal columns
     cum = tail2 + np.cumsum((s ** 2)[::-1])[::-1]
@@ -51,9 +68,9 @@ def qr_truncated_split(A, epsrel):
     return U, W[:, :kept].conj().T, kept, k
 
 
-def _check(theta, epsrel=1e-6):
+def _check(theta, epsrel=1e-6, delta=None):
     A = theta.conj().T if theta.shape[1] > theta.shape[0] else theta
-    U, C, kept, k = qr_truncated_split(A, epsrel)
+    U, C, kept, k = qr_truncated_split(A, epsrel, delta)
     s = np.linalg.svd(A, compute_uv=False)
     assert kept == to.truncation_rank(s, epsrel)
     err = np.linalg.norm(U @ C - A) / np.linalg.norm(A)
@@ -71,6 +88,18 @@ def test_random_graded_matrices():
         U = np.linalg.qr(rng.normal(size=(m, r)) + 1j * rng.normal(size=(m, r)))[0]
         V = np.linalg.qr(rng.normal(size=(n, r)) + 1j * rng.normal(size=(n, r)))[0]
         _check((U * sv) @ V.conj().T)
+        _check((U * sv) @ V.conj().T, delta=1e-14)
+
+
+def test_rank_deficient_and_tied_columns():
+    """Exactly repeated columns, zero columns and ties in the pivot search
+    (the lowest index wins) leave the kept rank and the reconstruction as
+    the full SVD's."""
+    rng = np.random.default_rng(1)
+    base = rng.normal(size=(24, 6)) + 1j * rng.normal(size=(24, 6))
+    A = np.concatenate([base, base, np.zeros((24, 3))], axis=1)
+    for delta in (None, 1e-14):
+        _check(A, delta=delta)
 
 
 def test_captured_tempo_bond_splits():
