@@ -193,7 +193,11 @@ class GpuPtTempoBackend:
         infl = np.array([self._influence(k) for k in range(self._num_infl)],
                         dtype=np.complex128)
         neg = None
-        first_neg = self._influence(-2)
+        # the grow phase (steps 2 .. num_steps - num_infl + 1) asks for the
+        # dk = -step influences (pt_tempo_backend.py:236-263); without a grow
+        # phase the reference never asks for them
+        grows = self._num_infl < self._num_steps
+        first_neg = self._influence(-2) if grows else None
         if first_neg is not None:
             D = self._d ** 2
             neg = np.zeros((self._num_steps + 1, D, D), dtype=np.complex128)

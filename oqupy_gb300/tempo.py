@@ -258,6 +258,10 @@ class GpuTempoBackend:
     def step(self):
         return self._step
 
+    def bond_dimensions(self) -> List[int]:
+        """Bond dimensions of the current MPS (sites - 1 values)."""
+        return self._batch.bond_dims(0)
+
     @property
     def chi_cap(self) -> int:
         """Current bond capacity of the device handle."""

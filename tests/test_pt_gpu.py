@@ -65,7 +65,7 @@ def test_gpu_pt_batched_builds():
 def test_gpu_pt_backend_dropin_matches_reference():
     """The drop-in backend driven like PtTempo.compute/get_process_tensor
     (pt_tempo.py:258-306), host tensors + caps as in the reference."""
-    from oqupy_gb300 import GpuPtTempoBackend, device_compute_dynamics
+    from oqupy_gb300 import GpuPtTempoBackend
     g = gc.load("nondiag_coupling")
     D = g["d"] ** 2
 
@@ -94,8 +94,8 @@ def test_gpu_pt_backend_dropin_matches_reference():
     host = to.compute_dynamics_pt(g["rho0"], gc.propagators(g), mpos, pt.caps,
                                   transform_in=pt.transform_in,
                                   transform_out=pt.transform_out)
-    dev = device_compute_dynamics(pt, [(g["prop1"][0], g["prop2"][0])],
-                                  [g["rho0"].reshape(-1)])[:, 0]
+    dev = be._batch.dynamics(0, g["prop1"][:1], g["prop2"][:1], g["rho0"].reshape(1, -1),
+                             transform_in=pt.transform_in, transform_out=pt.transform_out)[:, 0]
     for ref_states in (host, dev):
         errs = [to.trace_distance(a, b) for a, b in zip(ref_states, g["pt_states"][0])]
         assert not gc.parity_violations(errs, g["pt_envelope"][0])
