@@ -6,18 +6,23 @@ cutoff, H = Omega/2 sigma_x with Omega ~ U[0.5, 2], bath operator sigma_z/2,
 dkmax ~ U{20..300}, dt = 0.05, epsrel = 1e-6, 500 steps per trajectory,
 rho0 = spin up.  Inputs are synthetic (seeded draws of those distributions).
 
-One bench step = one TEMPO time step of every instance (one kernel launch).
-``value`` = instances x timed steps / 500 / timed seconds, i.e. whole
-trajectories per second at the cost of the timed steps; the per-step cost
-grows with the memory window (min(step, dkmax+1) sites) and the bonds, so the
-timed window is stated in ``config`` and ``--full-trajectories`` times all 500
-steps.  The headline form is "mixed" (pivoted QR + Jacobi and the
-contractions in double-float on the FP32 pipe, FP64 rank decisions and site
-storage); the complex128 form runs the same steps and the trace distance
-between the two is reported.
+One bench step = 25 TEMPO time steps of every instance (25 kernel launches),
+so ``--steps 20`` (the default) times whole 500-step trajectories and
+``value`` = whole trajectories per second of device time.  The headline form
+is "mixed" (pivoted QR + one-sided Jacobi and the contractions in
+double-float on the FP32 pipe; FP64 rank decisions and site storage); the
+complex128 form is timed on the first steps of the same instances, and the
+whole trajectories are compared with the FP64 oracle on a stratified
+subsample (committed fixture).  ``e2e`` is the same run through the host
+API, with every input uploaded and every state read back inside its timed
+region.
 
-``--impl reference`` times the CPU oracle (a plain-numpy restatement of the
-reference TEMPO backend) on the same workload and steps, on all host cores.
+``--impl reference`` runs the reference's own CPU implementation (the
+unmodified OQuPy TempoBackend from baseline/_ref when it is importable, else
+the plain-numpy port in oracle/) on a dkmax-stratified sample of the same
+batch, one single-threaded process per host core, and states the
+whole-trajectory throughput estimated from the measured prefixes.
+Other workloads: ``--workload pt | qutrit | surrogate``.
 """
 
 import argparse
@@ -32,14 +37,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 NSTEPS_TRAJ = 500
-DRAM_BYTES_PER_INSTANCE_STEP31 = (14.974464e6 + 0.60544e6) / 64
+BATCH_SEED = 20261203   # the benchmark batch (one batch, partitioned across ranks)
 METRIC = "spin-boson trajectories/sec on 1 GB300, mixed vs complex128, at 1e-6 trace dist"
-
-
-def rank_seed(rank):
-    """Every rank draws its own batch of independent instances (weak scaling:
-    the ranks share no data and exchange nothing but the timing reduction)."""
-    return 20261203 + rank
+CHUNK = 25              # TEMPO time steps per bench step: 20 bench steps = whole trajectories
 
 
 def max_over_ranks(seconds, world):
@@ -81,6 +81,129 @@ def make_instances(n, seed):
 # CPU oracle (reference arm / cpu_baseline)
 # ---------------------------------------------------------------------------
 
+def stratified_sample(insts, per=32):
+    """One instance per ``per``-instance stratum of the batch sorted by dkmax
+    (the stratum's middle element): the CPU legs' sample (16 of 512)."""
+    order = sorted(range(len(insts)), key=lambda i: (insts[i]["dkmax"], i))
+    return [order[min(k + per // 2, len(order) - 1)] for k in range(0, len(order), per)]
+
+
+def _prefix_worker(args):
+    """Steps 1, 2, ... of one instance on the CPU until ``budget`` seconds of
+    work are done or the trajectory is complete; per-step seconds.  ``kind``
+    "reference": the unmodified OQuPy TempoBackend (tempo_backend.py:577-626)
+    from baseline/_ref, its tensornetwork import served by the from-scratch
+    stand-in; "port": the plain-numpy oracle restatement."""
+    inst, budget, kind = args
+    import numpy as np
+    D = int(np.asarray(inst["rho0"]).size)
+    infl = inst["influences"]
+    influence = (lambda dk: infl[dk] if 0 <= dk < len(infl) else None)
+    props = (lambda step: (inst["prop1"], inst["prop2"]))
+    if kind == "reference":
+        for p in (os.path.join(ROOT, "oracle", "tnshim"), os.path.join(ROOT, "baseline", "_ref")):
+            if p not in sys.path:
+                sys.path.append(p)
+        import warnings
+        warnings.simplefilter("ignore")
+        from oqupy.backends.tempo_backend import TempoBackend
+        be = TempoBackend(np.asarray(inst["rho0"]).reshape(-1), influence, inst["unitary"], props,
+                          np.ones(D), np.ones(D), inst["dkmax"], inst["epsrel"], config={})
+    else:
+        from oracle import tempo_oracle as to
+        be = to.TempoOracle(np.asarray(inst["rho0"]).reshape(-1), influence, inst["unitary"], props,
+                            np.ones(D), np.ones(D), inst["dkmax"], inst["epsrel"])
+    be.initialize()
+    times, total = [], 0.0
+    while total < budget and len(times) < NSTEPS_TRAJ:
+        t0 = time.perf_counter()
+        be.compute_step()
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        total += dt
+    return times
+
+
+def reference_importable():
+    """True when the unmodified reference and its stand-in imports load."""
+    code = ("import sys, warnings; warnings.simplefilter('ignore'); "
+            f"sys.path += [{os.path.join(ROOT, 'oracle', 'tnshim')!r}, {os.path.join(ROOT, 'baseline', '_ref')!r}]; "
+            "from oqupy.backends.tempo_backend import TempoBackend")
+    try:
+        return subprocess.run([sys.executable, "-c", code], capture_output=True,
+                              timeout=300).returncode == 0
+    except Exception:
+        return False
+
+
+def extrapolate_trajectory(times, dkmax, nsteps=NSTEPS_TRAJ):
+    """Seconds of a whole ``nsteps``-step trajectory from the measured
+    per-step seconds of its first ``len(times)`` steps.  A TEMPO step's cost
+    grows with the memory window min(t, dkmax + 1) and is stationary once
+    the window is full: measured stationary steps are averaged; otherwise
+    the growth is a power law in the window, c(t) = c_m (w(t) / t_m)^g,
+    fitted (least squares in log-log) to the second half of the measured
+    steps, g clipped to [0.5, 3]."""
+    import numpy as np
+    tau = np.asarray(times, dtype=float)
+    tm = len(tau)
+    if tm >= nsteps:
+        return float(tau[:nsteps].sum())
+    full = dkmax + 1
+    if tm >= full:
+        # window full from step `full` on: the measured stationary steps
+        return float(tau.sum() + (nsteps - tm) * tau[max(full - 1, tm - 10):].mean())
+    lo = max(2, tm // 2)
+    x = np.log(np.arange(lo + 1, tm + 1, dtype=float))
+    y = np.log(np.maximum(tau[lo:], 1e-9))
+    g, c = np.polyfit(x, y, 1) if tm - lo >= 3 else (1.0, np.log(tau[-1]) - np.log(tm))
+    g = float(np.clip(g, 0.5, 3.0))
+    cm = float(np.exp(c + g * np.log(tm)))
+    t = np.arange(tm + 1, nsteps + 1, dtype=float)
+    return float(tau.sum() + np.sum(cm * (np.minimum(t, full) / tm) ** g))
+
+
+def cpu_whole_trajectories(insts, budget, kind, procs):
+    """Whole-trajectory throughput of the batch on ``procs`` host cores,
+    estimated from the stratified sample: each sampled instance runs from
+    step 1 in its own single-threaded process for ``budget`` seconds of
+    work; its whole-trajectory seconds are the measured prefix plus the
+    extrapolated rest (``extrapolate_trajectory``); the batch's CPU seconds
+    are the stratum sizes times the sampled instances' seconds."""
+    import multiprocessing as mp
+    import numpy as np
+    idx = stratified_sample(insts)
+    env_keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    old = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = "1"
+    try:
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(min(procs, len(idx))) as pool:
+            per = pool.map(_prefix_worker, [(insts[i], budget, kind) for i in idx], chunksize=1)
+        wall = time.perf_counter() - t0
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    whole = [extrapolate_trajectory(t, insts[i]["dkmax"]) for t, i in zip(per, idx)]
+    measured = [len(t) for t in per]
+    stratum = len(insts) / len(idx)
+    cpu_s = stratum * float(np.sum(whole))
+    rate = len(insts) / (cpu_s / procs)
+    frac = float(np.sum([sum(t) for t in per]) / np.sum(whole))
+    return {"value": rate, "unit": "trajectories/s", "cores": procs, "kind": kind,
+            "sample": (f"{len(idx)} instances (one per {stratum:.0f}-instance dkmax stratum of the batch), "
+                       f"each run from step 1 for {budget:.0f} s of single-threaded work (steps "
+                       f"{min(measured)}..{max(measured)} of {NSTEPS_TRAJ} measured), the rest of its "
+                       f"trajectory extrapolated by a power law in the memory window fitted to the "
+                       f"measured steps; {100 * frac:.0f}% of the estimated whole-trajectory seconds "
+                       f"measured; batch seconds = {stratum:.0f} x the sample's; {procs} cores"),
+            "measured_fraction": frac, "sample_steps_measured": measured, "wall_s": wall}
+
+
 def _oracle_worker(args):
     """Run one instance through the oracle: W untimed steps, K timed steps."""
     inst, warm, steps = args
@@ -100,25 +223,6 @@ def _oracle_worker(args):
     for _ in range(steps):
         o.compute_step()
     return time.perf_counter() - t0
-
-
-def cpu_oracle_latency(inst, warm, steps, threads):
-    """Latency mode: one instance in one process whose BLAS uses ``threads``
-    threads; returns the seconds of its ``steps`` timed steps."""
-    import multiprocessing as mp
-    env_keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
-    old = {k: os.environ.get(k) for k in env_keys}
-    for k in env_keys:
-        os.environ[k] = str(threads)
-    try:
-        with mp.get_context("spawn").Pool(1) as pool:
-            return float(pool.map(_oracle_worker, [(inst, warm, steps)])[0])
-    finally:
-        for k, v in old.items():
-            if v is None:
-                os.environ.pop(k, None)
-            else:
-                os.environ[k] = v
 
 
 def cpu_oracle_rate(insts, warm, steps, procs):
@@ -553,65 +657,266 @@ def run_qutrit(args):
     print(json.dumps(line))
 
 
-def run_full_trajectories(args, insts, workload):
-    """Mixed form over whole 500-step trajectories of the batch: 3 warm-up
-    steps on a separate batch, then a fresh batch timed step by step (CUDA
-    events on the launching stream, L2 flushed before every step)."""
+def _accuracy_vs_oracle(states, indices):
+    """Per-instance trace distance of whole trajectories against the FP64
+    oracle on the committed stratified subsample (tests/golden/
+    bench_oracle.npz, made by tests/golden/make_bench_oracle.py), beside
+    the oracle's own spread under 1e-15 / 1e-14 input perturbations."""
+    import numpy as np
+    path = os.path.join(ROOT, "tests", "golden", "bench_oracle.npz")
+    if not os.path.exists(path):
+        return None
+    g = np.load(path)
+    pos = {int(i): k for k, i in enumerate(indices)}
+    rows = []
+    for k, i in enumerate(g["index"]):
+        n = g["states"].shape[1]
+        if int(i) not in pos or states[pos[int(i)]].shape[0] < n:
+            continue
+        err = trace_distance_max(states[pos[int(i)]][:n], g["states"][k])
+        env = g["envelope"][k]
+        rows.append((int(i), int(g["dkmax"][k]), float(err.max()), float(env.max()),
+                     bool((err <= np.maximum(1e-6, 10 * env)).all())))
+    if not rows:
+        return None
+    e = np.array([r[2] for r in rows])
+    return {"instances": len(rows), "steps": int(g["states"].shape[1] - 1),
+            "frac_le_1e-6": float(np.mean(e <= 1e-6)),
+            "frac_le_max_1e-6_10x_envelope": float(np.mean([r[4] for r in rows])),
+            "median": float(np.median(e)), "max": float(e.max()),
+            "per_instance": [{"index": r[0], "dkmax": r[1], "max_trace_distance": r[2],
+                              "oracle_envelope_max": r[3]} for r in rows]}
+
+
+def run_tempo(args, rank, world):
+    """The headline workload: whole 500-step trajectories of the batch.
+
+    One bench step = ``CHUNK`` TEMPO time steps of every instance (one
+    kernel launch per time step); ``--steps 20`` is the whole trajectory.
+    Warm-up steps run on a separate batch of the same size and distribution
+    (its own seed), so the timed batch starts at step 1.  Timed region:
+    CUDA events on the launching stream around every launch (device time,
+    ``value``), nested in a wall-clock region (``e2e``) that also holds the
+    handle's creation from host arrays (influences, propagators, initial
+    states host->device) and the read-back of every bench step's states
+    device->host.  L2 is flushed before every bench step (the batch's site
+    rings are also far larger than L2).  Several ranks: one batch, the
+    instances partitioned by predicted cost (oqupy_gb300.multigpu), states
+    gathered to rank 0 on the host.
+    """
     import numpy as np
     import torch
-    from oqupy_gb300 import TempoBatch
-    stream = torch.cuda.current_stream()
+    from oqupy_gb300 import TempoBatch, _native
+    from oqupy_gb300 import multigpu as mg
+    dev_stream = torch.cuda.current_stream()
+    shape = dict(chi_cap=args.chi_cap, qr_cut=args.qr_cut, block=args.block, smem_kb=args.smem_kb)
+    t_setup = time.perf_counter()
+    insts = make_instances(args.instances, BATCH_SEED)
+    setup_s = time.perf_counter() - t_setup       # influences + propagators on the host
+    if world > 1:
+        costs = mg.probe_costs(insts, steps=20)
+        parts = mg.lpt_partition(costs, world)
+    else:
+        parts = [list(range(len(insts)))]
+    local = [insts[i] for i in parts[rank]]
+    total_steps = min(args.steps * CHUNK, NSTEPS_TRAJ)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    cap = max(args.chi_cap, 96)           # bonds keep growing past the default window
-    w = TempoBatch(insts, precision="mixed", chi_cap=cap, out_cap=4)
-    for _ in range(max(3, args.warmup if args.warmup < 10 else 3)):
-        w.advance(1, stream.cuda_stream)
+    # warm-up: W bench steps of a separate batch
+    warm = TempoBatch(make_instances(len(local), BATCH_SEED + 7919), precision="mixed",
+                      out_cap=2, **shape)
+    for _ in range(args.warmup):
+        warm.advance(CHUNK, dev_stream.cuda_stream)
     torch.cuda.synchronize()
-    w.close()
-    b = TempoBatch(insts, precision="mixed", chi_cap=cap, out_cap=NSTEPS_TRAJ + 1)
+    warm.check_status()
+    warm.close()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    D = 4
+    states = np.zeros((len(local), total_steps + 1, D), dtype=np.complex128)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(NSTEPS_TRAJ)]
+          for _ in range(total_steps)]
     clocks = ClockSampler()
-    torch.cuda.synchronize()
+    barrier()
     clocks.start()
-    for k in range(NSTEPS_TRAJ):
+    t0 = time.perf_counter()
+    b = TempoBatch(local, precision="mixed", out_cap=CHUNK + 1, **shape)
+    h2d = sum(np.asarray(x["influences"]).nbytes + np.asarray(x["prop1"]).nbytes
+              + np.asarray(x["prop2"]).nbytes + np.asarray(x["rho0"]).nbytes for x in local)
+    d2h = 0
+    states[:, 0] = np.array([np.asarray(x["rho0"]).reshape(-1) for x in local])
+    done = 0
+    for k in range(args.steps):
+        n = min(CHUNK, total_steps - done)
+        if n <= 0:
+            break
         flush.zero_()
-        ev[k][0].record(stream)
-        b.advance(1, stream.cuda_stream)
-        ev[k][1].record(stream)
+        for j in range(n):
+            ev[done + j][0].record(dev_stream)
+            b.advance(1, dev_stream.cuda_stream)
+            ev[done + j][1].record(dev_stream)
+        chunk_states = b.states(done + 1, n)             # device -> host (synchronises)
+        states[:, done + 1: done + 1 + n] = chunk_states
+        d2h += chunk_states.nbytes
+        done += n
     torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
     clk = clocks.stop()
-    ms = np.array([a.elapsed_time(c) for a, c in ev])
     b.check_status()
+    ms = np.array([e0.elapsed_time(e1) for e0, e1 in ev[:done]])
     infos = [b.info(i) for i in range(b.n)]
     b.close()
-    total = float(ms.sum()) / 1e3
-    line = {"metric": METRIC, "value": len(insts) / total, "unit": "trajectories/s", "n_gpus": 1,
-            "steps": NSTEPS_TRAJ, "warmup": 3, "ms_per_step": float(ms.mean()), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (Jacobi in double-float)",
-            "data": "synthetic",
-            "config": dict(workload, timed_steps=f"1..{NSTEPS_TRAJ} (whole trajectories)", precision="mixed"),
-            "ms_per_step_by_block": [float(ms[i:i + 50].mean()) for i in range(0, NSTEPS_TRAJ, 50)],
-            "max_bond": max(int(x["max_bond"]) for x in infos),
-            "splits": int(sum(x["splits"] for x in infos)), "clocks": clk,
-            "gpu_launches": NSTEPS_TRAJ}
+    flops = float(sum(x["flops_alg"] for x in infos))
+    dev_s = max_over_ranks(float(ms.sum()) / 1e3, world)
+    e2e_all = max_over_ranks(e2e_s, world)
+    frac_traj = done / NSTEPS_TRAJ
+    value = len(insts) * frac_traj / dev_s
+    all_states = mg.gather_rows(states, parts, len(insts), rank, world)
+
+    # complex128 on the first steps of the same instances (both forms' event
+    # times over the same launches)
+    c128 = None
+    nc = min(args.c128_steps, done)
+    if nc > 0 and not args.no_complex128:
+        bc = TempoBatch(local, precision="complex128", out_cap=nc + 1, **shape)
+        evc = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(nc)]
+        torch.cuda.synchronize()
+        for j in range(nc):
+            if j % CHUNK == 0:
+                flush.zero_()
+            evc[j][0].record(dev_stream)
+            bc.advance(1, dev_stream.cuda_stream)
+            evc[j][1].record(dev_stream)
+        torch.cuda.synchronize()
+        bc.check_status()
+        msc = np.array([e0.elapsed_time(e1) for e0, e1 in evc])
+        st_c = bc.states(0, nc + 1)
+        ic = [bc.info(i) for i in range(bc.n)]
+        bc.close()
+        td = trace_distance_max(states[:, : nc + 1], st_c).max(axis=1)
+        t_mixed = float(ms[:nc].sum())
+        t_c = float(msc.sum())
+        c128 = {"steps": f"1..{nc}", "complex128_ms_per_step": t_c / nc, "mixed_ms_per_step": t_mixed / nc,
+                "mixed_speedup_vs_complex128": t_c / t_mixed,
+                "mixed_vs_complex128_trace_distance": {
+                    "max": float(td.max()), "median": float(np.median(td)),
+                    "frac_le_1e-6": float(np.mean(td <= 1e-6))},
+                "complex128_sweeps64_per_split": sum(x["sweeps64"] for x in ic) / max(1, sum(x["splits"] for x in ic))}
+
+    nsplit = max(1, sum(x["splits"] for x in infos))
+    stats = {"max_bond": max(x["max_bond"] for x in infos), "splits": nsplit,
+             "sweeps64_per_split": sum(x["sweeps64"] for x in infos) / nsplit,
+             "sweepsff_per_split": sum(x["sweeps32"] for x in infos) / nsplit}
+    if rank != 0:
+        return
+    peak_fp32 = _native.fma_peak_tflops(1)
+    achieved = flops / (float(ms.sum()) / 1e3) / 1e12
+    roofline = {"bound": "fp32-pipe", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+                "frac": achieved / peak_fp32, "traffic": None,
+                "kernel": "tempo_kernel<true> (QR + double-float Jacobi bond splits)",
+                "achieved_def": ("algorithmic flops of the timed launches (complex R-SVD count "
+                                 "4 (6 R N^2 + 20 N^3) per split of an R x N matrix + 8 per complex "
+                                 "multiply-add of the contractions) / their summed event time"),
+                "peak_source": "measured FFMA throughput of this GPU (otb_measure_fma_peak); "
+                               "the bound is the FP32 pipe the double-float arithmetic runs on",
+                "traffic_note": ("DRAM bytes vary with the memory window over a trajectory; the "
+                                 "ncu capture of one launch (step 31, 64 instances) is in profiles/")}
+    cpu = None
+    if world == 1 and args.cpu_sample > 0:
+        cpu = cpu_whole_trajectories(insts, args.cpu_budget, "port", os.cpu_count() or 1)
+    acc = _accuracy_vs_oracle(all_states, list(range(len(insts)))) if all_states is not None else None
+    line = {"metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(ms.sum()) / max(1, args.steps),
+            "higher_is_better": True, "scaling": "strong" if world > 1 else "weak",
+            "vs_baseline": None, "dtype": "c128 storage; splits and contractions in double-float (f32 pairs)",
+            "data": "synthetic (seeded draws of the batched spin-boson distribution)",
+            "config": {"workload": (f"batched TEMPO spin-boson, {len(insts)} instances (alpha U[0.01,0.5], "
+                                    "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
+                                    "epsrel 1e-6), whole 500-step trajectories"),
+                       "instances": len(insts), "seed": BATCH_SEED,
+                       "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
+                       "timed_steps": f"1..{done} of {NSTEPS_TRAJ}",
+                       "warmup": f"{args.warmup} bench steps on a separate batch (seed {BATCH_SEED + 7919})",
+                       "l2": "flushed (256 MiB write) before every bench step; site rings >> L2",
+                       "precision": "mixed", "parallelism": f"instances x {world} GPUs",
+                       "launch": {"block": args.block or 256, "smem_kb": args.smem_kb or 56}},
+            "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": {"value": len(insts) * frac_traj / e2e_all, "unit": "trajectories/s",
+                    "h2d_bytes_per_step": int(h2d // max(1, args.steps)),
+                    "d2h_bytes_per_step": int(d2h // max(1, args.steps)),
+                    "note": ("same run, wall clock: handle creation from host arrays (all inputs "
+                             "host->device), every launch, every bench step's states device->host")},
+            "clocks": clk, "gpu_launches": int(done), "mixed_stats": stats,
+            "setup_seconds": setup_s,
+            "ms_per_step_by_block": [float(ms[i:i + 50].sum()) / len(ms[i:i + 50]) for i in range(0, done, 50)],
+            "accuracy_vs_fp64_oracle": acc}
+    if c128:
+        line["complex128_window"] = c128
+    print(json.dumps(line))
+
+
+def run_reference(args, rank, world):
+    """``--impl reference``: the reference's own CPU implementation on the
+    same batch and metric, all host cores, rank 0 only."""
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    t_setup = time.perf_counter()
+    insts = make_instances(args.instances, BATCH_SEED)
+    setup_s = time.perf_counter() - t_setup
+    kind = "reference" if reference_importable() else "port"
+    cpu = cpu_whole_trajectories(insts, args.ref_budget, kind, procs)
+    value = cpu["value"]
+    line = {"metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * args.instances / value / NSTEPS_TRAJ * CHUNK,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded draws of the batched spin-boson distribution)",
+            "config": {"workload": (f"batched TEMPO spin-boson, {args.instances} instances (alpha U[0.01,0.5], "
+                                    "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
+                                    "epsrel 1e-6), whole 500-step trajectories"),
+                       "instances": args.instances, "seed": BATCH_SEED,
+                       "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
+                       "timed_steps": f"1..{min(args.steps * CHUNK, NSTEPS_TRAJ)} of {NSTEPS_TRAJ}",
+                       "warmup": "none (CPU)", "l2": "n/a (CPU)",
+                       "precision": "complex128", "parallelism": f"one single-threaded process per core x {procs}"},
+            "impl": "reference",
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": value, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "setup_seconds": setup_s,
+            "measured_fraction": cpu["measured_fraction"],
+            "sample_steps_measured": cpu["sample_steps_measured"]}
     print(json.dumps(line))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20,
+                    help=f"timed bench steps; one bench step = {CHUNK} TEMPO time steps of the batch "
+                         f"(20 = whole {NSTEPS_TRAJ}-step trajectories)")
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--instances", type=int, default=512)
-    ap.add_argument("--cpu-sample", type=int, default=512)
+    ap.add_argument("--cpu-sample", type=int, default=1,
+                    help="0: skip the CPU baseline of the gb300 line")
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU work per sampled instance (cpu_baseline)")
+    ap.add_argument("--ref-budget", type=float, default=60.0,
+                    help="seconds of CPU work per sampled instance (--impl reference)")
     ap.add_argument("--no-complex128", action="store_true")
+    ap.add_argument("--c128-steps", type=int, default=50,
+                    help="first TEMPO steps timed in the complex128 form for the comparison")
     ap.add_argument("--chi-cap", type=int, default=64)
+    ap.add_argument("--block", type=int, default=0, help="threads per CTA (0 = the library default)")
+    ap.add_argument("--smem-kb", type=int, default=0, help="dynamic shared memory per CTA (0 = default)")
     ap.add_argument("--qr-cut", type=float, default=0.0,
                     help="relative cut of the bond split's QR (0 = the precision form's default)")
-    ap.add_argument("--full-trajectories", action="store_true",
-                    help="time whole 500-step trajectories of the batch (mixed form only)")
     ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit"])
     ap.add_argument("--qutrit-instances", type=int, default=128)
     ap.add_argument("--qutrit-chi-cap", type=int, default=96)
@@ -632,7 +937,6 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    seed = rank_seed(rank)
     if args.workload == "qutrit":
         if rank != 0:
             return
@@ -660,145 +964,15 @@ def main():
             return
         run_surrogate(args)
         return
-
-    workload = {"workload": f"batched TEMPO spin-boson, {args.instances} instances (alpha U[0.01,0.5], "
-                            "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, "
-                            "dt 0.05, epsrel 1e-6, 500-step trajectories)",
-                "instances_per_gpu": args.instances,
-                "timed_steps": f"{args.warmup + 1}..{args.warmup + args.steps} of {NSTEPS_TRAJ}",
-                "l2": "flushed (256 MiB write) before every timed step",
-                "seed": seed}
-
     if args.impl == "reference":
-        if rank != 0:
-            return
-        t_setup = time.perf_counter()
-        insts = make_instances(args.instances, seed)
-        setup_s = time.perf_counter() - t_setup
-        procs = os.cpu_count() or 1
-        rate, cpu_s, wall = cpu_oracle_rate(insts, args.warmup, args.steps, procs)
-        per_step_ms = cpu_s / procs / args.steps * 1e3
-        # latency mode: the instance with the longest memory alone, BLAS on all cores
-        big = max(insts, key=lambda i: i["dkmax"])
-        lat_s = cpu_oracle_latency(big, args.warmup, args.steps, procs)
-        line = {"metric": METRIC, "value": rate, "unit": "trajectories/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step_ms,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "c128", "data": "synthetic", "config": workload, "impl": "reference",
-                "cpu_baseline": {"value": rate, "unit": "trajectories/s", "cores": procs,
-                                 "kind": "port",
-                                 "sample": f"{len(insts)} instances x steps {args.warmup + 1}.."
-                                           f"{args.warmup + args.steps}, numpy oracle, one "
-                                           f"single-threaded process per core"},
-                "e2e": {"value": rate, "unit": "trajectories/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0},
-                "setup_seconds": setup_s,
-                "latency_mode": {"value": args.steps / NSTEPS_TRAJ / lat_s, "unit": "trajectories/s",
-                                 "ms_per_step": lat_s / args.steps * 1e3, "threads": procs,
-                                 "sample": f"one instance (dkmax {big['dkmax']}) x steps "
-                                           f"{args.warmup + 1}..{args.warmup + args.steps}, "
-                                           "BLAS threads = all cores"}}
-        print(json.dumps(line))
+        run_reference(args, rank, world)
         return
-
-    import numpy as np
     import torch
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    from oqupy_gb300 import _native
-    t_setup = time.perf_counter()
-    insts = make_instances(args.instances, seed)
-    setup_s = time.perf_counter() - t_setup        # influences + propagators on the host
-    if args.full_trajectories:
-        if rank == 0:
-            run_full_trajectories(args, insts, workload)
-        return
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    clocks = ClockSampler()
-    barrier()
-    clocks.start()
-    t_mixed, ms_mixed, fl_mixed, st_mixed, stats_mixed, e2e_m = run_gpu_form(
-        torch, insts, "mixed", args.warmup, args.steps, flush, args.chi_cap, args.steps, args.qr_cut)
-    clk = clocks.stop()
-    barrier()
-    t_mixed_s = max_over_ranks(t_mixed / 1e3, world)
-    value = world * args.instances * args.steps / NSTEPS_TRAJ / t_mixed_s
-
-    res = {}
-    if not args.no_complex128:
-        t_c, ms_c, fl_c, st_c, stats_c, _ = run_gpu_form(torch, insts, "complex128",
-                                                          args.warmup, args.steps, flush,
-                                                          args.chi_cap)
-        td = trace_distance_max(st_mixed, st_c).max(axis=1)
-        res = {"complex128_value": world * args.instances * args.steps / NSTEPS_TRAJ / (t_c / 1e3),
-               "complex128_ms_per_step": t_c / args.steps,
-               "mixed_speedup_vs_complex128": t_c / t_mixed,
-               "mixed_vs_complex128_trace_distance": {
-                   "max": float(td.max()), "median": float(np.median(td)),
-                   "frac_le_1e-6": float(np.mean(td <= 1e-6))},
-               "complex128_stats": stats_c}
-
-    e2e_s, h2d, d2h = e2e_m
-    e2e = {"value": world * args.instances * args.steps / NSTEPS_TRAJ / e2e_s,
-           "unit": "trajectories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "note": (f"steps {args.warmup + 1}..{args.warmup + args.steps} (the timed window, on a "
-                    "second batch advanced through the same warm-up) through the plugin path: "
-                    "all propagators host->device in one call, one launch, the new states "
-                    "device->host; wall clock")}
-    peak_fp32 = _native.fma_peak_tflops(1)
-    peak_fp64 = _native.fma_peak_tflops(0)
-    achieved = fl_mixed / t_mixed_s / 1e12
-    roofline = {"bound": "fp32-pipe", "achieved": achieved, "peak": peak_fp32,
-                "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
-                "kernel": "tempo_kernel<true> (double-float Jacobi)",
-                "achieved_def": "algorithmic flops (complex R-SVD count per split + contractions) / event time",
-                "peak_source": "measured FFMA throughput (otb_measure_fma_peak)",
-                "fp64_pipe_peak_tflops": peak_fp64}
-    if res:
-        ach_c = fl_c / (t_c / 1e3) / 1e12
-        roofline["complex128"] = {"bound": "fp64-pipe", "achieved": ach_c, "peak": peak_fp64,
-                                  "frac": ach_c / peak_fp64}
-    # DRAM bytes per launch: ncu capture of the mixed kernel at step 31 for the
-    # first 64 instances of this batch (dram__bytes_read.sum + write = 15.58 MB),
-    # scaled by the instance count (every instance reads and writes only its
-    # own site ring, influences and states)
-    roofline["traffic"] = DRAM_BYTES_PER_INSTANCE_STEP31 * args.instances
-    roofline["traffic_source"] = ("ncu, step 31, 64 instances, scaled by instances "
-                                  "(profiles/tempo_kernel_mixed_step31.md)")
-
-    cpu = None
-    if rank == 0 and world == 1 and args.cpu_sample > 0:
-        procs = os.cpu_count() or 1
-        sample = insts[: args.cpu_sample]
-        rate, cpu_s, wall = cpu_oracle_rate(sample, args.warmup, args.steps, procs)
-        cpu = {"value": rate, "unit": "trajectories/s", "cores": procs, "kind": "port",
-               "sample": f"{len(sample)} instances x steps {args.warmup + 1}..{args.warmup + args.steps}"
-                         f" ({cpu_s:.1f} CPU-s), numpy oracle, one process per core"}
-
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "trajectories/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (Jacobi in double-float)",
-                "data": "synthetic", "config": dict(workload, precision="mixed",
-                                                    parallelism=f"instances x {world} GPUs"),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk, "gpu_launches": args.steps, "mixed_stats": stats_mixed,
-                "setup_seconds": setup_s,
-                "whole_trajectories": ("value is trajectory-equivalents at the cost of the timed "
-                                       "steps; per-step cost grows ~15x over a 500-step trajectory "
-                                       "(longer memory windows, larger bonds): whole trajectories "
-                                       "are timed by `python bench.py --full-trajectories`")}
-        line.update(res)
-        print(json.dumps(line))
+    run_tempo(args, rank, world)
     if world > 1:
         torch.distributed.destroy_process_group()
 

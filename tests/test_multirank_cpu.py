@@ -1,14 +1,13 @@
-"""Multi-rank host logic of the benchmark on CPU (gloo, world size 2):
-independent per-rank batches, the max-over-ranks timing reduction, and a
-reference arm that prints from rank 0 only under torchrun."""
+"""Multi-rank host logic of the benchmark on CPU (gloo, world size 2): the
+max-over-ranks timing reduction, a reference arm that prints from rank 0
+only under torchrun, and the whole-trajectory extrapolation of the CPU legs.
+The partition of one batch across ranks is covered by
+tests/test_multigpu_cpu.py."""
 import json
 import os
 import socket
 import subprocess
 import sys
-
-import numpy as np
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -28,11 +27,11 @@ def _worker(rank, world, port, q):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench
     got = bench.max_over_ranks(1.0 + 2.5 * rank, world)
-    q.put((rank, got, bench.rank_seed(rank)))
+    q.put((rank, got))
     dist.destroy_process_group()
 
 
-def test_max_over_ranks_and_per_rank_seeds_with_gloo():
+def test_max_over_ranks_with_gloo():
     import torch.multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -46,22 +45,13 @@ def test_max_over_ranks_and_per_rank_seeds_with_gloo():
         assert p.exitcode == 0
     res.sort()
     assert [r[1] for r in res] == [3.5, 3.5]          # both ranks see the slowest
-    assert res[0][2] != res[1][2]                     # independent batches
-
-
-def test_rank_batches_are_independent_draws():
-    sys.path.insert(0, ROOT)
-    import bench
-    a = bench.make_instances(3, bench.rank_seed(0))
-    b = bench.make_instances(3, bench.rank_seed(1))
-    assert not np.allclose(a[0]["prop1"], b[0]["prop1"]) or a[0]["dkmax"] != b[0]["dkmax"]
 
 
 def test_reference_arm_under_torchrun_prints_once():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--instances", "2", "--steps", "1", "--warmup", "3"]
+           "--instances", "2", "--steps", "1", "--warmup", "3", "--ref-budget", "2"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
@@ -69,3 +59,17 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0 and line["n_gpus"] == 2
+    assert line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_trajectory_extrapolation_on_a_known_cost_law():
+    """Per-step cost that grows with the memory window and is stationary
+    once it is full: the estimate from a prefix equals the whole sum."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for dk in (25, 180, 290):
+        true = [2e-3 * min(t, dk + 1) ** 1.3 for t in range(1, bench.NSTEPS_TRAJ + 1)]
+        for tm in (15, 90, 260):
+            est = bench.extrapolate_trajectory(true[:tm], dk)
+            assert abs(est / sum(true) - 1) < 0.02, (dk, tm, est / sum(true))
