@@ -61,7 +61,7 @@ typedef struct {
   int32_t chi_cap;     /* bond-dimension capacity of every site, chi_cap * D <= 1152 */
   int32_t out_cap;     /* states kept per instance (ring), >= 2 */
   int32_t grid;        /* CTAs per launch, 0 = 3 per SM */
-  int32_t block;       /* threads per CTA (64..256, multiple of 32), 0 = 256 */
+  int32_t block;       /* threads per CTA (64..512, multiple of 32), 0 = 256 */
   int32_t smem_kb;     /* dynamic shared memory per CTA for working matrices
                           (KiB, <= 200), 0 = 56 */
   double qr_cut;       /* relative cut of the rank-revealing QR that precedes

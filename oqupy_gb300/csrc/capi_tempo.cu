@@ -137,8 +137,8 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   if (cfg->chi_cap < 4 || cfg->chi_cap > 1152)
     return set_error(OTB_ERR_INVALID_ARG, "chi_cap must be in [4, 1152 / D]");
   if (cfg->out_cap < 2) return set_error(OTB_ERR_INVALID_ARG, "out_cap must be >= 2");
-  if (cfg->block != 0 && (cfg->block < 64 || cfg->block > 256 || cfg->block % 32 != 0))
-    return set_error(OTB_ERR_INVALID_ARG, "block must be 0 or a multiple of 32 in [64, 256]");
+  if (cfg->block != 0 && (cfg->block < 64 || cfg->block > 512 || cfg->block % 32 != 0))
+    return set_error(OTB_ERR_INVALID_ARG, "block must be 0 or a multiple of 32 in [64, 512]");
   if (cfg->smem_kb < 0 || cfg->smem_kb > 200)
     return set_error(OTB_ERR_INVALID_ARG, "smem_kb must be in [0, 200]");
   if (!(cfg->qr_cut >= 0.0) || !(cfg->qr_cut < 1.0))
@@ -262,9 +262,10 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // default launch shape (measured best of the shapes the autotuner tries on
-  // the batched configuration): 3 CTAs of 256 threads per SM, 56 KiB smem
-  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, 3 * std::max(sms, 1)));
+  // default launch shape: 3 CTAs of 256 threads per SM with 56 KiB smem;
+  // CTAs of more than 256 threads (128 registers each) fill an SM alone
+  const int per_sm = h->block > 256 ? 1 : 3;
+  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, per_sm * std::max(sms, 1)));
   if (h->smem_bytes == 0) h->smem_bytes = 56 * 1024;
   h->wcap = (long long)(h->cap * h->Dmax) * (h->cap * h->Dmax);
   h->work_stride = tempo_work_bytes(h->wcap);

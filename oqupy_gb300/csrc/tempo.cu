@@ -40,7 +40,8 @@
 
 namespace otb {
 
-constexpr int TEMPO_THREADS = 256;
+constexpr int TEMPO_THREADS = 512;   // largest CTA of the batched kernel (launch bound)
+constexpr int STATIC_THREADS = 256;  // CTA of the allocation-free single-instance kernel
 constexpr int NMAX = 1152;   // max columns of a split (D * cap <= 1152)
 
 typedef cx<double> zc;
@@ -628,7 +629,7 @@ constexpr long long STATIC_SCRATCH_BYTES = STATIC_WCAP * (3 * 16 + 16);
 static __device__ __align__(256) unsigned char g_tempo_static_scratch[STATIC_SCRATCH_BYTES];
 
 template <bool MIXED>
-__global__ void __launch_bounds__(TEMPO_THREADS)
+__global__ void __launch_bounds__(STATIC_THREADS)
     tempo_static_kernel(TempoLaunch L, InstDev I, const double* rho0, int nsteps, int* status_out) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ SharedStep sh;
@@ -744,10 +745,10 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
   cudaError_t e;
   if (io->precision == 0) {
     e = cudaFuncSetAttribute(tempo_static_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) tempo_static_kernel<false><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
+    if (e == cudaSuccess) tempo_static_kernel<false><<<1, STATIC_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
   } else {
     e = cudaFuncSetAttribute(tempo_static_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) tempo_static_kernel<true><<<1, TEMPO_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
+    if (e == cudaSuccess) tempo_static_kernel<true><<<1, STATIC_THREADS, smem, s>>>(L, I, io->rho0, nsteps, io->status_out);
   }
   if (e == cudaSuccess) e = cudaGetLastError();
   if (!check_cuda(e, "otb_tempo_advance_static launch")) return OTB_ERR_CUDA;

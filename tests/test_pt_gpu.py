@@ -9,9 +9,7 @@ from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
 
-# D=4 fixtures.  The D=9 builds and the reduced config-2 build (bond
-# dimension 168: 672-column splits) are FP64-bound on the single CTA that
-# owns an instance and take minutes; they are not part of this suite.
+# D=4 fixtures; the big-bond and qutrit builds have their own tests below.
 PT_CASES = ["ref_spin_boson_A", "nondiag_coupling", "add_corr_time"]
 
 
@@ -99,3 +97,35 @@ def test_gpu_pt_backend_dropin_matches_reference():
     for ref_states in (host, dev):
         errs = [to.trace_distance(a, b) for a, b in zip(ref_states, g["pt_states"][0])]
         assert not gc.parity_violations(errs, g["pt_envelope"][0])
+
+
+@pytest.mark.parametrize("precision", ["complex128", "mixed"])
+def test_gpu_pt_build_big_bonds(precision):
+    """The process-tensor model of the big PT configuration (alpha 0.3,
+    wc 5, T 1, dt 0.02, epsrel 1e-7) at dkmax 20 and 50 steps: bonds reach
+    168, so the zip-up splits have up to 672 columns.  Bond profile and the
+    dynamics of three Hamiltonians against the reference."""
+    import time
+    from oqupy_gb300 import PtBatch
+    g = gc.load("pt_config2_small")
+    t0 = time.perf_counter()
+    b = PtBatch([_inst(g)], precision=precision, chi_cap=192)
+    b.build()
+    dt = time.perf_counter() - t0
+    bonds = list(b.bond_dimensions(0))
+    print(f"pt_config2_small {precision}: build {dt:.1f} s, max bond {max(bonds)}")
+    if precision == "complex128" and float(g["pt_envelope"].max()) < 1e-10:
+        assert bonds == list(g["pt_bonds"])
+    _check(b, 0, g, gc.PARITY_ABS if precision == "complex128" else gc.MIXED_ABS)
+
+
+def test_gpu_pt_build_qutrit():
+    """A D = 9 process tensor (mixed form; bonds reach 105, splits of up to
+    945 columns) and its dynamics.  (The qutrit_superohmic fixture's process
+    tensor reaches bond 320, 2880-column splits, past the 1152-column limit
+    of a split on one CTA.)"""
+    from oqupy_gb300 import PtBatch
+    g = gc.load("ref_qutrit_C")
+    b = PtBatch([_inst(g)], precision="mixed", chi_cap=128)
+    b.build()
+    _check(b, 0, g, gc.MIXED_ABS)
