@@ -69,6 +69,8 @@ struct QA<double> {
   }
   static __device__ __forceinline__ E conj(const E& x) { return mk<double>(x.x, -x.y); }
   static __device__ __forceinline__ E zeroE() { return mk<double>(0.0, 0.0); }
+  static __device__ __forceinline__ E oneE() { return mk<double>(1.0, 0.0); }
+  static __device__ __forceinline__ E mulc(const E& a, const E& b) { return cmul(a, b); }
 };
 
 template <>
@@ -106,6 +108,18 @@ struct QA<ff> {
     E r;
     r.x = ff_make(0.f, 0.f);
     r.y = r.x;
+    return r;
+  }
+  static __device__ __forceinline__ E oneE() {
+    E r;
+    r.x = ff_make(1.f, 0.f);
+    r.y = ff_make(0.f, 0.f);
+    return r;
+  }
+  static __device__ __forceinline__ E mulc(const E& a, const E& b) {
+    E r;
+    r.x = ff_sub(ff_mul(a.x, b.x), ff_mul(a.y, b.y));
+    r.y = ff_add(ff_mul(a.x, b.y), ff_mul(a.y, b.x));
     return r;
   }
 };
@@ -265,6 +279,125 @@ __device__ int qrcp_inplace(typename QA<T>::E* X, int R, int N, float delta, flo
   return k;
 }
 
+// Unpivoted Householder QR of Z (M x K, M >= K, column-major ld), in place,
+// one __syncthreads per column: on return the upper triangle of Z[0:K, :]
+// holds R, below the diagonal column i holds its reflector w_i scaled to
+// w_i[i] = 1 (implicit), and tau[i] (FP64) makes H_i = I - tau_i w_i w_i^H,
+// Z = H_0 H_1 ... H_{K-1} [R; 0].  The reflector scalars are computed by
+// every warp from column i, which no thread writes during step i; column
+// i's scaling and diagonal are written in step i + 1, when no warp reads it.
+template <typename T>
+__device__ void householder_unit(typename QA<T>::E* Z, int M, int K, int ld, double* tau) {
+  typedef QA<T> Q;
+  typedef typename Q::E E;
+  typedef typename Q::S S;
+  const int tid = threadIdx.x, nt = blockDim.x, lane32 = tid & 31;
+  E pinv = Q::zeroE(), palpha = Q::zeroE();   // previous column's 1 / v_i and diagonal
+  for (int i = 0; i < K; ++i) {
+    if (i > 0) {
+      E* c = Z + (size_t)(i - 1) * ld;
+      for (int r = i + tid; r < M; r += nt) c[r] = Q::mulc(c[r], pinv);
+      if (tid == 0) c[i - 1] = palpha;
+    }
+    const E* v = Z + (size_t)i * ld;
+    S n2 = Q::zero();
+    for (int r = i + lane32; r < M; r += 32) n2 = Q::abs2_acc(v[r], n2);
+    for (int off = 16; off > 0; off >>= 1) n2 = Q::add(n2, Q::shfl(n2, off));
+    double s0x = 0.0, s0y = 0.0, sb = 0.0, sax = 0.0, say = 0.0, ivx = 0.0, ivy = 0.0, st = 0.0;
+    if (lane32 == 0) {
+      const double nrm = sqrt(fmax(Q::tod(n2), 0.0));
+      const cx<double> x0 = Q::to(v[i]);
+      const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
+      const double ex = (a0 > 0.0) ? x0.x / a0 : 1.0, ey = (a0 > 0.0) ? x0.y / a0 : 0.0;
+      const double m = a0 + nrm;   // |v_i|
+      s0x = ex * m;
+      s0y = ey * m;
+      sb = (nrm > 0.0) ? 1.0 / (nrm * m) : 0.0;
+      sax = -ex * nrm;
+      say = -ey * nrm;
+      ivx = (m > 0.0) ? ex / m : 0.0;   // 1 / v_i = conj(e) / |v_i|
+      ivy = (m > 0.0) ? -ey / m : 0.0;
+      st = (nrm > 0.0) ? m / nrm : 0.0;  // tau = beta |v_i|^2
+    }
+    s0x = __shfl_sync(0xffffffffu, s0x, 0);
+    s0y = __shfl_sync(0xffffffffu, s0y, 0);
+    sb = __shfl_sync(0xffffffffu, sb, 0);
+    sax = __shfl_sync(0xffffffffu, sax, 0);
+    say = __shfl_sync(0xffffffffu, say, 0);
+    ivx = __shfl_sync(0xffffffffu, ivx, 0);
+    ivy = __shfl_sync(0xffffffffu, ivy, 0);
+    if (tid == 0) tau[i] = st;
+    pinv = Q::from(mk<double>(ivx, ivy));
+    palpha = Q::from(mk<double>(sax, say));
+    const E v0 = Q::from(mk<double>(s0x, s0y));
+    const S beta = Q::fromd(sb);
+    const int G = jacobi_group(M - i);
+    const int gl = tid & (G - 1), group = tid / G, ngroups = nt / G;
+    const int nrest = K - i - 1;
+    for (int tb = 0; tb < nrest; tb += ngroups) {
+      const int t = tb + group;
+      const bool act = t < nrest;
+      E* cj = Z + (size_t)(act ? i + 1 + t : i) * ld;
+      S wr = Q::zero(), wi = Q::zero();
+      if (act) {
+        for (int r = i + gl; r < M; r += G) Q::dotj(wr, wi, (r == i) ? v0 : v[r], cj[r]);
+      }
+      for (int off = G >> 1; off > 0; off >>= 1) {
+        wr = Q::add(wr, Q::shfl(wr, off));
+        wi = Q::add(wi, Q::shfl(wi, off));
+      }
+      if (act) {
+        const S bx = Q::mul(beta, wr), by = Q::mul(beta, wi);
+        for (int r = i + gl; r < M; r += G) cj[r] = Q::sub_scaled(cj[r], (r == i) ? v0 : v[r], bx, by);
+      }
+    }
+    __syncthreads();
+  }
+  if (K > 0) {
+    E* c = Z + (size_t)(K - 1) * ld;
+    for (int r = K + tid; r < M; r += nt) c[r] = Q::mulc(c[r], pinv);
+    if (tid == 0) c[K - 1] = palpha;
+  }
+  __syncthreads();
+}
+
+// Y <- Q Y for the first ncols columns of Y (M x ncols, ld ldy), Q = H_0 ...
+// H_{K-1} as stored by householder_unit: reflectors applied last-first, one
+// __syncthreads each.
+template <typename T>
+__device__ void apply_q_unit(const typename QA<T>::E* Z, int M, int K, int ld, const double* tau,
+                             typename QA<T>::E* Y, int ncols, int ldy) {
+  typedef QA<T> Q;
+  typedef typename Q::E E;
+  typedef typename Q::S S;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const E one = Q::oneE();
+  for (int i = K - 1; i >= 0; --i) {
+    const E* w = Z + (size_t)i * ld;
+    const S ti = Q::fromd(tau[i]);
+    const int G = jacobi_group(M - i);
+    const int gl = tid & (G - 1), group = tid / G, ngroups = nt / G;
+    for (int jb = 0; jb < ncols; jb += ngroups) {
+      const int j = jb + group;
+      const bool act = j < ncols;
+      E* y = Y + (size_t)(act ? j : 0) * ldy;
+      S sr = Q::zero(), si = Q::zero();
+      if (act) {
+        for (int r = i + gl; r < M; r += G) Q::dotj(sr, si, (r == i) ? one : w[r], y[r]);
+      }
+      for (int off = G >> 1; off > 0; off >>= 1) {
+        sr = Q::add(sr, Q::shfl(sr, off));
+        si = Q::add(si, Q::shfl(si, off));
+      }
+      if (act) {
+        const S bx = Q::mul(ti, sr), by = Q::mul(ti, si);
+        for (int r = i + gl; r < M; r += G) y[r] = Q::sub_scaled(y[r], (r == i) ? one : w[r], bx, by);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // The split driver.  W (R x N, FP64, ld R) holds the oriented matrix and is
 // scratch afterwards; X (R x N elements of QA<T>::E) is the QR workspace; zs /
 // zs_bytes is spare shared memory for the Jacobi operand.  delta <= 0 selects
@@ -315,6 +448,57 @@ __device__ int qr_jacobi_truncate(cx<double>* W, int R, int N, typename QA<T>::E
   int sw, sw64 = 0;
   bool done;
   cx<double>* O = reinterpret_cast<cx<double>*>(X);
+  if (k >= 8 && 2 * k <= N) {
+    // Second (unpivoted) QR, Z = Q2 [R2; 0]: the Jacobi runs on the k x k R2
+    // instead of the N rows of Z, the rank is decided from R2's singular
+    // values (those of Z), and W = Q2 [W2; 0] is formed for the kept columns
+    // only, in sorted order.  X's storage: [0, N kk) the kept columns,
+    // [N k, N k + k^2) R2, then tau (k doubles): N k + k^2 + k <= R N for
+    // 2 k <= N <= R.
+    E* R2 = X + (size_t)N * k;
+    double* tau = reinterpret_cast<double*>(X + (size_t)N * k + (size_t)k * k);
+    householder_unit<T>(Z, N, k, N, tau);
+    for (int idx = tid; idx < k * k; idx += nt) {
+      const int c = idx / k, r = idx - c * k;
+      R2[idx] = (r <= c) ? Z[(size_t)c * N + r] : Q::zeroE();
+    }
+    __syncthreads();
+    cx<double>* R2d = reinterpret_cast<cx<double>*>(R2);
+    if (FF) {
+      sw = jacobi_sweeps_ff(reinterpret_cast<cff*>(R2), k, k, k, sh);
+      done = sw < JACOBI_MAX_SWEEPS || sh->noise_converged;
+      for (int idx = tid; idx < k * k; idx += nt) R2d[idx] = cscale(Q::to(R2[idx]), scale);
+      __syncthreads();
+      if (!done) sw64 = jacobi_sweeps<double>(R2d, k, k, k, nullptr, 0, sh);
+    } else {
+      sw64 = jacobi_sweeps<double>(R2d, k, k, k, nullptr, 0, sh);
+      sw = 0;
+      for (int idx = tid; idx < k * k; idx += nt) R2d[idx] = cscale(R2d[idx], scale);
+      __syncthreads();
+    }
+    if (tid == 0) sh->sweeps32 = sw;
+    const int kk = jacobi_finish<double>(R2d, k, k, k, epsrel, norm, perm, sh, sw64,
+                                         (double)tail2 * scale * scale);
+    if (tid == 0) sh->sweeps = sw64;
+    E* Y = X;
+    for (int idx = tid; idx < N * kk; idx += nt) {
+      const int j = idx / N, r = idx - j * N;
+      Y[idx] = (r < k) ? Q::from(cscale(R2d[(size_t)perm[j] * k + r], inv)) : Q::zeroE();
+    }
+    __syncthreads();
+    apply_q_unit<T>(Z, N, k, N, tau, Y, kk, N);
+    for (int idx = tid; idx < N * kk; idx += nt) O[idx] = cscale(Q::to(Y[idx]), scale);
+    // the kept columns are stored sorted: norms in that order, identity perm
+    for (int j = tid; j < kk; j += nt) tau[j] = norm[perm[j]];
+    __syncthreads();
+    for (int j = tid; j < kk; j += nt) {
+      norm[j] = tau[j];
+      perm[j] = j;
+    }
+    __syncthreads();
+    *Wout = O;
+    return kk;
+  }
   if (FF) {
     sw = jacobi_sweeps_ff(reinterpret_cast<cff*>(Z), N, k, N, sh);
     done = sw < JACOBI_MAX_SWEEPS || sh->noise_converged;

@@ -60,12 +60,74 @@ def qr_truncated_split(A, epsrel, delta=None):
         for q in range(N):
             if colstep[q] >= i:
                 Z[q, i] = np.conj(X[i, q])
+    _last_Z["Z"], _last_Z["tail2"] = Z.copy(), tail2
     u, s, vh = np.linalg.svd(Z, full_matrices=False)
     W = u * s                                        # Z V: orthogonal columns
     cum = tail2 + np.cumsum((s ** 2)[::-1])[::-1]
     kept = max(1, int(np.sum(np.sqrt(cum) > epsrel * s[0])))
     U = A @ W[:, :kept] / s[:kept] ** 2
     return U, W[:, :kept].conj().T, kept, k
+
+
+def householder_unit(Z):
+    """Unpivoted Householder QR of Z (M x K, M >= K) as the kernel stores it:
+    R in the upper triangle, below the diagonal the reflector w_i scaled to
+    w_i[i] = 1, tau_i real with H_i = I - tau_i w_i w_i^H (the kernel writes
+    the scaled column one step late, which changes no number)."""
+    Z = np.array(Z, dtype=np.complex128)
+    M, K = Z.shape
+    tau = np.zeros(K)
+    for i in range(K):
+        x = Z[i:, i].copy()
+        nrm = np.linalg.norm(x)
+        a0 = abs(x[0])
+        e = x[0] / a0 if a0 > 0 else 1.0
+        v0 = e * (a0 + nrm)
+        beta = 1.0 / (nrm * (nrm + a0)) if nrm > 0 else 0.0
+        v = x.copy()
+        v[0] = v0
+        for j in range(i + 1, K):
+            w = np.vdot(v, Z[i:, j])
+            Z[i:, j] -= beta * v * w
+        tau[i] = beta * abs(v0) ** 2
+        Z[i + 1:, i] = x[1:] / v0 if nrm > 0 else 0.0
+        Z[i, i] = -e * nrm
+    return Z, tau
+
+
+def apply_q(Zf, tau, Y):
+    """Q Y with Q = H_0 H_1 ... H_{K-1} (reflectors applied last-first)."""
+    M, K = Zf.shape
+    Y = np.array(Y, dtype=np.complex128)
+    for i in reversed(range(K)):
+        w = np.concatenate([[1.0], Zf[i + 1:, i]])
+        s = w.conj() @ Y[i:, :]
+        Y[i:, :] -= tau[i] * np.outer(w, s)
+    return Y
+
+
+def lq_reduced_split(A, epsrel, delta=None):
+    """The kernel's branch for k <= N / 2: Z = Q2 [R2; 0] by a second
+    (unpivoted) Householder QR, the SVD of the k x k R2 (exact here, one-sided
+    Jacobi on the GPU), the rank decision from R2's singular values, and
+    W = Q2 [W2; 0] formed for the kept columns only."""
+    U, C, kept, k = qr_truncated_split(A, epsrel, delta)      # the QR and Z
+    N = A.shape[1]
+    Zfull, tail2 = _last_Z["Z"], _last_Z["tail2"]
+    Zf, tau = householder_unit(Zfull)
+    R2 = np.triu(Zf[:k, :k])
+    u, s, vh = np.linalg.svd(R2)
+    W2 = u * s                                          # R2 V: orthogonal columns
+    cum = tail2 + np.cumsum((s ** 2)[::-1])[::-1]
+    kk = max(1, int(np.sum(np.sqrt(cum) > epsrel * s[0])))
+    Y = np.zeros((N, kk), dtype=np.complex128)
+    Y[:k] = W2[:, :kk]
+    W = apply_q(Zf, tau, Y)                             # = Z V[:, :kk] = A^H U S
+    Uk = A @ W / s[:kk] ** 2
+    return Uk, W.conj().T, kk, k
+
+
+_last_Z = {}
 
 
 def _check(theta, epsrel=1e-6, delta=None):
@@ -131,3 +193,31 @@ def test_captured_tempo_bond_splits():
     ks = [_check(th) for th in captured[::5]]
     # the rank-revealing cut shrinks the Jacobi problem on these matrices
     assert np.mean([k / n for k, n in ks]) < 0.95
+
+
+def test_second_qr_reduction_of_the_jacobi_operand():
+    """k <= N / 2: the Jacobi runs on the k x k R2 of Z = Q2 [R2; 0]; kept
+    rank and reconstruction equal the full SVD's."""
+    rng = np.random.default_rng(5)
+    n_lq = 0
+    for _ in range(20):
+        m, n = rng.integers(24, 90, size=2)
+        r = min(m, n)
+        # fast geometric decay (TEMPO bond spectra): about half the values
+        # above the mixed form's QR cut
+        sv = 10.0 ** (-np.linspace(0, rng.uniform(18, 30), r))
+        U = np.linalg.qr(rng.normal(size=(m, r)) + 1j * rng.normal(size=(m, r)))[0]
+        V = np.linalg.qr(rng.normal(size=(n, r)) + 1j * rng.normal(size=(n, r)))[0]
+        theta = (U * sv) @ V.conj().T
+        A = theta.conj().T if theta.shape[1] > theta.shape[0] else theta
+        for delta in (None, 1e-14):
+            Uk, C, kept, k = lq_reduced_split(A, 1e-6, delta)
+            if 2 * k > A.shape[1]:
+                continue
+            n_lq += 1
+            s = np.linalg.svd(A, compute_uv=False)
+            assert kept == to.truncation_rank(s, 1e-6)
+            err = np.linalg.norm(Uk @ C - A) / np.linalg.norm(A)
+            trunc = np.sqrt(np.sum(s[kept:] ** 2)) / np.linalg.norm(A)
+            assert err <= 1.01 * trunc + 1e-12
+    assert n_lq > 10
