@@ -61,6 +61,23 @@ __device__ __forceinline__ ff ff_rsqrt(ff u) {
   return ff_add(y, ff_mul(ff_make(0.5f * y0, 0.f), e));
 }
 
+// sqrt(u) for u >= 0: the IEEE float square root refined by one Newton step
+// in FF (y + (u - y^2) / (2 y)); 0 for u <= 0
+__device__ __forceinline__ ff ff_sqrt(ff u) {
+  if (!(u.hi > 0.f)) return ff_make(0.f, 0.f);
+  const float y = __fsqrt_rn(u.hi);
+  const ff e = ff_sub(u, ff_mul(ff_make(y, 0.f), ff_make(y, 0.f)));
+  return ff_add(ff_make(y, 0.f), ff_make(__fdiv_rn(e.hi, 2.f * y), 0.f));
+}
+
+// 1 / b for b != 0: the IEEE float reciprocal refined by one Newton step in
+// FF (y + y (1 - b y))
+__device__ __forceinline__ ff ff_recip(ff b) {
+  const float y = __fdiv_rn(1.f, b.hi);
+  const ff e = ff_sub(ff_make(1.f, 0.f), ff_mul(b, ff_make(y, 0.f)));
+  return ff_add(ff_make(y, 0.f), ff_mul(ff_make(y, 0.f), e));
+}
+
 __device__ __forceinline__ ff ff_shfl_xor(ff v, int off) {
   return ff_make(__shfl_xor_sync(0xffffffffu, v.hi, off, 32), __shfl_xor_sync(0xffffffffu, v.lo, off, 32));
 }

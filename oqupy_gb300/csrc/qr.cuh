@@ -43,6 +43,18 @@ namespace otb {
 template <typename T>
 struct QA;
 
+// Householder scalars of a column x (rows i..) with head x0 and squared norm
+// n2: v0 = e (|x0| + |x|), alpha = -e |x| (the new diagonal), beta =
+// 1 / (|x| (|x| + |x0|)) (H = I - beta v v^H), inv = 1 / v0, tau = beta |v0|^2
+// (the unit-diagonal form), e = x0 / |x0| (1 for x0 = 0); a zero column gives
+// H = I.
+template <typename E, typename S>
+struct Refl {
+  E v0, alpha, inv;
+  S beta;
+  double tau;
+};
+
 template <>
 struct QA<double> {
   typedef cx<double> E;  // element of the working matrix
@@ -71,6 +83,33 @@ struct QA<double> {
   static __device__ __forceinline__ E zeroE() { return mk<double>(0.0, 0.0); }
   static __device__ __forceinline__ E oneE() { return mk<double>(1.0, 0.0); }
   static __device__ __forceinline__ E mulc(const E& a, const E& b) { return cmul(a, b); }
+  // FP64: evaluated by one lane of each warp and broadcast (the FP64 pipe is
+  // the narrow one)
+  static constexpr bool kAllLanes = false;
+  static __device__ __forceinline__ Refl<E, S> reflector(S n2, const E& x0) {
+    Refl<E, S> r;
+    const double nrm = sqrt(fmax(n2, 0.0));
+    const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
+    const double ex = (a0 > 0.0) ? x0.x / a0 : 1.0, ey = (a0 > 0.0) ? x0.y / a0 : 0.0;
+    const double m = a0 + nrm;
+    r.v0 = mk<double>(ex * m, ey * m);
+    r.alpha = mk<double>(-ex * nrm, -ey * nrm);
+    r.inv = (m > 0.0) ? mk<double>(ex / m, -ey / m) : mk<double>(0.0, 0.0);
+    r.beta = (nrm > 0.0) ? 1.0 / (nrm * m) : 0.0;
+    r.tau = (nrm > 0.0) ? m / nrm : 0.0;
+    return r;
+  }
+  static __device__ __forceinline__ Refl<E, S> bcast(Refl<E, S> r) {
+    r.v0.x = __shfl_sync(0xffffffffu, r.v0.x, 0);
+    r.v0.y = __shfl_sync(0xffffffffu, r.v0.y, 0);
+    r.alpha.x = __shfl_sync(0xffffffffu, r.alpha.x, 0);
+    r.alpha.y = __shfl_sync(0xffffffffu, r.alpha.y, 0);
+    r.inv.x = __shfl_sync(0xffffffffu, r.inv.x, 0);
+    r.inv.y = __shfl_sync(0xffffffffu, r.inv.y, 0);
+    r.beta = __shfl_sync(0xffffffffu, r.beta, 0);
+    r.tau = __shfl_sync(0xffffffffu, r.tau, 0);
+    return r;
+  }
 };
 
 template <>
@@ -122,6 +161,42 @@ struct QA<ff> {
     r.y = ff_add(ff_mul(a.x, b.y), ff_mul(a.y, b.x));
     return r;
   }
+  // double-float on the FP32 pipe: evaluated by every lane (n2 and x0 are
+  // the same in all lanes), no FP64 instruction and no broadcast
+  static constexpr bool kAllLanes = true;
+  static __device__ __forceinline__ Refl<E, S> reflector(S n2, const E& x0) {
+    Refl<E, S> r;
+    const ff z = ff_make(0.f, 0.f);
+    const ff nrm = ff_sqrt(n2);
+    const ff a0 = ff_sqrt(ff_fma(x0.x, x0.x, ff_mul(x0.y, x0.y)));
+    ff ex = ff_make(1.f, 0.f), ey = z;
+    if (a0.hi > 0.f) {
+      const ff ia = ff_recip(a0);
+      ex = ff_mul(x0.x, ia);
+      ey = ff_mul(x0.y, ia);
+    }
+    const ff m = ff_add(a0, nrm);
+    r.v0.x = ff_mul(ex, m);
+    r.v0.y = ff_mul(ey, m);
+    r.alpha.x = ff_make(-ff_mul(ex, nrm).hi, -ff_mul(ex, nrm).lo);
+    r.alpha.y = ff_make(-ff_mul(ey, nrm).hi, -ff_mul(ey, nrm).lo);
+    r.inv.x = z;
+    r.inv.y = z;
+    r.beta = z;
+    r.tau = 0.0;
+    if (m.hi > 0.f) {
+      const ff im = ff_recip(m);
+      r.inv.x = ff_mul(ex, im);
+      const ff t = ff_mul(ey, im);
+      r.inv.y = ff_make(-t.hi, -t.lo);
+    }
+    if (nrm.hi > 0.f) {
+      r.beta = ff_recip(ff_mul(nrm, m));
+      r.tau = ff_to(ff_mul(m, ff_recip(nrm)));
+    }
+    return r;
+  }
+  static __device__ __forceinline__ Refl<E, S> bcast(Refl<E, S> r) { return r; }
 };
 
 // Default relative cut of the QR (the remaining block's Frobenius norm over
@@ -212,27 +287,15 @@ __device__ int qrcp_inplace(typename QA<T>::E* X, int R, int N, float delta, flo
     S n2 = Q::zero();
     for (int r = i + lane32; r < R; r += 32) n2 = Q::abs2_acc(v[r], n2);
     for (int off = 16; off > 0; off >>= 1) n2 = Q::add(n2, Q::shfl(n2, off));
-    double s0x = 0.0, s0y = 0.0, sb = 0.0, sax = 0.0, say = 0.0;
-    if (lane32 == 0) {
-      const double nrm = sqrt(fmax(Q::tod(n2), 0.0));
-      const cx<double> x0 = Q::to(v[i]);
-      const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
-      const double ex = (a0 > 0.0) ? x0.x / a0 : 1.0, ey = (a0 > 0.0) ? x0.y / a0 : 0.0;
-      s0x = ex * (a0 + nrm);
-      s0y = ey * (a0 + nrm);
-      sb = (nrm > 0.0) ? 1.0 / (nrm * (nrm + a0)) : 0.0;
-      sax = -ex * nrm;
-      say = -ey * nrm;
-    }
-    s0x = __shfl_sync(0xffffffffu, s0x, 0);
-    s0y = __shfl_sync(0xffffffffu, s0y, 0);
-    sb = __shfl_sync(0xffffffffu, sb, 0);
+    Refl<E, S> rf;
+    if (Q::kAllLanes || lane32 == 0) rf = Q::reflector(n2, v[i]);
+    rf = Q::bcast(rf);
     if (tid == 0) {
       pend_p = p;
-      pend_a = Q::from(mk<double>(sax, say));
+      pend_a = rf.alpha;
     }
-    const E v0 = Q::from(mk<double>(s0x, s0y));
-    const S beta = Q::fromd(sb);
+    const E v0 = rf.v0;
+    const S beta = rf.beta;
     // (c) apply H to the other unchosen columns (list positions i..N-1 but
     // pos), refresh their partial norms (rows > i) in the other buffer
     const int G = jacobi_group(R - i);
@@ -303,34 +366,14 @@ __device__ void householder_unit(typename QA<T>::E* Z, int M, int K, int ld, dou
     S n2 = Q::zero();
     for (int r = i + lane32; r < M; r += 32) n2 = Q::abs2_acc(v[r], n2);
     for (int off = 16; off > 0; off >>= 1) n2 = Q::add(n2, Q::shfl(n2, off));
-    double s0x = 0.0, s0y = 0.0, sb = 0.0, sax = 0.0, say = 0.0, ivx = 0.0, ivy = 0.0, st = 0.0;
-    if (lane32 == 0) {
-      const double nrm = sqrt(fmax(Q::tod(n2), 0.0));
-      const cx<double> x0 = Q::to(v[i]);
-      const double a0 = sqrt(x0.x * x0.x + x0.y * x0.y);
-      const double ex = (a0 > 0.0) ? x0.x / a0 : 1.0, ey = (a0 > 0.0) ? x0.y / a0 : 0.0;
-      const double m = a0 + nrm;   // |v_i|
-      s0x = ex * m;
-      s0y = ey * m;
-      sb = (nrm > 0.0) ? 1.0 / (nrm * m) : 0.0;
-      sax = -ex * nrm;
-      say = -ey * nrm;
-      ivx = (m > 0.0) ? ex / m : 0.0;   // 1 / v_i = conj(e) / |v_i|
-      ivy = (m > 0.0) ? -ey / m : 0.0;
-      st = (nrm > 0.0) ? m / nrm : 0.0;  // tau = beta |v_i|^2
-    }
-    s0x = __shfl_sync(0xffffffffu, s0x, 0);
-    s0y = __shfl_sync(0xffffffffu, s0y, 0);
-    sb = __shfl_sync(0xffffffffu, sb, 0);
-    sax = __shfl_sync(0xffffffffu, sax, 0);
-    say = __shfl_sync(0xffffffffu, say, 0);
-    ivx = __shfl_sync(0xffffffffu, ivx, 0);
-    ivy = __shfl_sync(0xffffffffu, ivy, 0);
-    if (tid == 0) tau[i] = st;
-    pinv = Q::from(mk<double>(ivx, ivy));
-    palpha = Q::from(mk<double>(sax, say));
-    const E v0 = Q::from(mk<double>(s0x, s0y));
-    const S beta = Q::fromd(sb);
+    Refl<E, S> rf;
+    if (Q::kAllLanes || lane32 == 0) rf = Q::reflector(n2, v[i]);
+    rf = Q::bcast(rf);
+    if (tid == 0) tau[i] = rf.tau;
+    pinv = rf.inv;
+    palpha = rf.alpha;
+    const E v0 = rf.v0;
+    const S beta = rf.beta;
     const int G = jacobi_group(M - i);
     const int gl = tid & (G - 1), group = tid / G, ngroups = nt / G;
     const int nrest = K - i - 1;

@@ -78,7 +78,7 @@ struct SharedStep {
 constexpr int QR_MIN_COLS = 8;
 
 template <bool MIXED>
-__device__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel, float qr_delta,
+__device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel, float qr_delta,
                      Bufs& b, SharedStep& sh, zc** Wout, bool* flip) {
   const int tid = threadIdx.x, nt = blockDim.x;
   size_t used = 0;
@@ -552,7 +552,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(TEMPO_THREADS) tempo_kernel(TempoLaunch L) {
+__global__ void __launch_bounds__(TEMPO_THREADS, 1) tempo_kernel(TempoLaunch L) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ SharedStep sh;
   Bufs b;
