@@ -735,6 +735,8 @@ def run_tempo(args, rank, world):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    from oqupy_gb300.autotune import BucketTuner
+    tuner = BucketTuner() if args.autotune else None
     D = 4
     states = np.zeros((len(local), total_steps + 1, D), dtype=np.complex128)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -754,13 +756,21 @@ def run_tempo(args, rank, world):
         if n <= 0:
             break
         flush.zero_()
+        if tuner is not None:
+            tuner.begin_chunk(b.max_bond() if done else 1)
+        shape = None
         for j in range(n):
+            if tuner is not None and tuner.shape_for(j) != shape:
+                shape = tuner.shape_for(j)
+                b.set_launch(shape[0], shape[1])
             ev[done + j][0].record(dev_stream)
             b.advance(1, dev_stream.cuda_stream)
             ev[done + j][1].record(dev_stream)
         chunk_states = b.states(done + 1, n)             # device -> host (synchronises)
         states[:, done + 1: done + 1 + n] = chunk_states
         d2h += chunk_states.nbytes
+        if tuner is not None:
+            tuner.end_chunk([e0.elapsed_time(e1) for e0, e1 in ev[done: done + n]])
         done += n
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -843,7 +853,8 @@ def run_tempo(args, rank, world):
                        "warmup": f"{args.warmup} bench steps on a separate batch (seed {BATCH_SEED + 7919})",
                        "l2": "flushed (256 MiB write) before every bench step; site rings >> L2",
                        "precision": "mixed", "parallelism": f"instances x {world} GPUs",
-                       "launch": {"block": args.block or 256, "smem_kb": args.smem_kb or 56}},
+                       "launch": ({"autotuned_per_bond_bucket": tuner.table()} if tuner is not None
+                                  else {"block": args.block or 256, "smem_kb": args.smem_kb or 56})},
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": len(insts) * frac_traj / e2e_all, "unit": "trajectories/s",
                     "h2d_bytes_per_step": int(h2d // max(1, args.steps)),
@@ -914,6 +925,8 @@ def main():
                     help="first TEMPO steps timed in the complex128 form for the comparison")
     ap.add_argument("--chi-cap", type=int, default=64)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0 = the library default)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="fixed launch shape instead of the per-bond-bucket tuner")
     ap.add_argument("--smem-kb", type=int, default=0, help="dynamic shared memory per CTA (0 = default)")
     ap.add_argument("--qr-cut", type=float, default=0.0,
                     help="relative cut of the bond split's QR (0 = the precision form's default)")

@@ -107,6 +107,13 @@ void otb_tempo_destroy(otb_tempo* h);
 /* Replaces nsteps calls of TempoBackend.compute_step (tempo_backend.py:619-626)
  * for every instance of the handle. */
 otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stream);
+/* Launch shape of the next advances (no reference counterpart: the
+ * reference has no launch): block threads per CTA (64..512, 0 = 256),
+ * smem_kb dynamic shared memory per CTA (<= 200, 0 = 56), grid CTAs (0 = 3
+ * per SM for blocks up to 256 threads, 1 per SM above; capped at the grid
+ * the handle's workspace was allocated for).  Used by the per-bond-bucket
+ * launch-shape tuner. */
+otb_status otb_tempo_set_launch(otb_tempo* h, int32_t block, int32_t smem_kb, int32_t grid);
 /* States of steps [first_step, first_step+count) of one instance, each D
  * complex; steps must still be held by the output ring (step 0 = rho0). */
 otb_status otb_tempo_read_states(otb_tempo* h, int32_t inst, int32_t first_step,

@@ -111,6 +111,7 @@ def _declare(lib):
         "otb_tempo_set_all_propagators": (i32, [P, c_double_p, c_double_p, P]),
         "otb_tempo_set_first_influence": (i32, [P, i32, c_double_p]),
         "otb_tempo_reserve_sites": (i32, [P, i32]),
+        "otb_tempo_set_launch": (i32, [P, i32, i32, i32]),
         "otb_pt_create": (i32, [ctypes.POINTER(PtConfig), i32,
                                 ctypes.POINTER(PtInstance), ctypes.POINTER(P)]),
         "otb_pt_destroy": (None, [P]),
@@ -148,7 +149,7 @@ def exported_symbols():
         "otb_tempo_read_states", "otb_tempo_read_all_states",
         "otb_tempo_get_info", "otb_tempo_bond_dims", "otb_tempo_set_influence",
         "otb_tempo_set_propagators", "otb_tempo_set_all_propagators", "otb_tempo_set_first_influence",
-        "otb_tempo_reserve_sites", "otb_pt_create", "otb_pt_destroy",
+        "otb_tempo_reserve_sites", "otb_tempo_set_launch", "otb_pt_create", "otb_pt_destroy",
         "otb_pt_advance", "otb_pt_get_info", "otb_pt_bond_dims",
         "otb_pt_get_tensor", "otb_pt_get_cap", "otb_dyn_run", "otb_mlp_gemm",
         "otb_mlp_transpose_bf16", "otb_mlp_f32_to_bf16", "otb_mlp_colsum",

@@ -1,12 +1,21 @@
-"""Launch-shape autotuner for the batched TEMPO kernel.
+"""Launch-shape autotuners for the batched TEMPO kernel.
 
 The bond splits of one instance run on one CTA, so the free parameters are
 the CTA width, how many CTAs share an SM and how much shared memory each gets
 for working matrices (matrices that do not fit stay in global memory behind
-L1/L2).  The best choice depends on the bond dimensions of the batch.
-``tune`` times each candidate shape on a sample of the batch for a few steps
-from the start and returns the fastest; results can be cached per
-(D, dkmax bucket) in a JSON file.
+L1/L2).  The best choice depends on the bond dimensions, which grow over a
+trajectory: while they are small the batch is throughput-bound (many narrow
+CTAs win); once they are large the step is bound by the few largest
+instances' split latency (one wide CTA per SM wins).
+
+* ``BucketTuner`` (used on the product path by ``bench.py``): the shape is
+  chosen per bond bucket of the running batch.  The first chunk of steps
+  spent in a new bucket alternates the candidate shapes launch by launch
+  (every tuning launch is a real step of the run), and the faster shape
+  serves the rest of the bucket.
+* ``tune``: times each candidate shape on a sample of the batch for a few
+  steps from the start and returns the fastest; results can be cached per
+  (D, dkmax bucket) in a JSON file.
 """
 
 import json
@@ -19,6 +28,54 @@ from .tempo import TempoBatch
 # (threads per CTA, CTAs per SM, dynamic smem KiB)
 CANDIDATES: List[Tuple[int, int, int]] = [
     (256, 3, 56), (256, 2, 88), (256, 1, 200), (192, 3, 56), (128, 4, 48)]
+
+
+# (threads per CTA, dynamic smem KiB): narrow CTAs, three per SM / one wide CTA per SM
+BUCKET_CANDIDATES: List[Tuple[int, int]] = [(256, 56), (512, 200)]
+
+
+class BucketTuner:
+    """Launch shape per bond bucket (``bucket_width`` bond values each).
+
+    ``shape_for(step_in_chunk)`` gives the shape of a launch in the current
+    chunk; ``end_chunk(times)`` takes the chunk's per-launch event times and
+    settles an untuned bucket (mean time per shape over its interleaved
+    launches); ``begin_chunk(max_bond)`` selects the bucket of the next
+    chunk.  Pure policy: the caller applies shapes (``TempoBatch.set_launch``)
+    and times launches."""
+
+    def __init__(self, candidates: Sequence[Tuple[int, int]] = BUCKET_CANDIDATES,
+                 bucket_width: int = 8):
+        self.candidates = list(candidates)
+        self.width = int(bucket_width)
+        self.best: Dict[int, Tuple[int, int]] = {}
+        self.trials: Dict[int, Dict[Tuple[int, int], float]] = {}
+        self.bucket = 0
+
+    def begin_chunk(self, max_bond: int):
+        self.bucket = int(max_bond) // self.width
+
+    def tuning(self) -> bool:
+        return self.bucket not in self.best
+
+    def shape_for(self, k: int) -> Tuple[int, int]:
+        if self.tuning():
+            return self.candidates[k % len(self.candidates)]
+        return self.best[self.bucket]
+
+    def end_chunk(self, times_ms: Sequence[float]):
+        if not self.tuning() or not times_ms:
+            return
+        acc: Dict[Tuple[int, int], List[float]] = {}
+        for k, t in enumerate(times_ms):
+            acc.setdefault(self.shape_for(k), []).append(float(t))
+        means = {c: sum(v) / len(v) for c, v in acc.items()}
+        self.trials[self.bucket] = means
+        self.best[self.bucket] = min(means, key=means.get)
+
+    def table(self) -> Dict[str, List[int]]:
+        return {f"bond {b * self.width}-{b * self.width + self.width - 1}": list(c)
+                for b, c in sorted(self.best.items())}
 
 
 def _sm_count() -> int:

@@ -19,6 +19,8 @@ struct otb_tempo {
   int cap = 0;
   int out_cap = 0;
   int grid = 0;
+  int grid_alloc = 0;   // CTAs the per-CTA workspace is allocated for
+  int sms = 0;
   int block = 256;
   int smem_bytes = 0;
   int Dmax = 0;
@@ -265,11 +267,15 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
   // default launch shape: 3 CTAs of 256 threads per SM with 56 KiB smem;
   // CTAs of more than 256 threads (128 registers each) fill an SM alone
   const int per_sm = h->block > 256 ? 1 : 3;
-  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, per_sm * std::max(sms, 1)));
+  h->sms = std::max(sms, 1);
+  h->grid = cfg->grid > 0 ? cfg->grid : std::max(1, std::min(n, per_sm * h->sms));
+  // workspace for the widest default grid, so otb_tempo_set_launch can
+  // switch shapes later (an explicit grid fixes it)
+  h->grid_alloc = cfg->grid > 0 ? cfg->grid : std::max(h->grid, std::min(n, 3 * h->sms));
   if (h->smem_bytes == 0) h->smem_bytes = 56 * 1024;
   h->wcap = (long long)(h->cap * h->Dmax) * (h->cap * h->Dmax);
   h->work_stride = tempo_work_bytes(h->wcap);
-  if (!h->d_work.alloc((size_t)h->grid * h->work_stride)) return OTB_ERR_OOM;
+  if (!h->d_work.alloc((size_t)h->grid_alloc * h->work_stride)) return OTB_ERR_OOM;
   *out = h.release();
   return OTB_OK;
 }
@@ -314,6 +320,20 @@ extern "C" otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stre
   L.smem_bytes = 0;
   if (!check_cuda(launch_tempo(L, h->precision, h->grid, h->block, h->smem_bytes, s), "tempo launch"))
     return OTB_ERR_CUDA;
+  return OTB_OK;
+}
+
+extern "C" otb_status otb_tempo_set_launch(otb_tempo* h, int32_t block, int32_t smem_kb, int32_t grid) {
+  if (!h) return set_error(OTB_ERR_INVALID_ARG, "null handle");
+  if (block != 0 && (block < 64 || block > 512 || block % 32 != 0))
+    return set_error(OTB_ERR_INVALID_ARG, "block must be 0 or a multiple of 32 in [64, 512]");
+  if (smem_kb < 0 || smem_kb > 200) return set_error(OTB_ERR_INVALID_ARG, "smem_kb must be in [0, 200]");
+  if (grid < 0) return set_error(OTB_ERR_INVALID_ARG, "grid must be >= 0");
+  h->block = block > 0 ? block : 256;
+  h->smem_bytes = (smem_kb > 0 ? smem_kb : 56) * 1024;
+  const int per_sm = h->block > 256 ? 1 : 3;
+  const int want = grid > 0 ? grid : std::min(h->n, per_sm * h->sms);
+  h->grid = std::max(1, std::min(want, h->grid_alloc));
   return OTB_OK;
 }
 

@@ -215,6 +215,14 @@ class TempoBatch:
             m = nat.cplx(mat)
             nat.check(nat.lib().otb_tempo_set_first_influence(self._h, int(i), nat.dptr(m)))
 
+    def set_launch(self, block: int = 0, smem_kb: int = 0, grid: int = 0):
+        """Launch shape of the next ``advance`` calls (``otb_tempo_set_launch``)."""
+        nat.check(nat.lib().otb_tempo_set_launch(self._h, int(block), int(smem_kb), int(grid)))
+
+    def max_bond(self) -> int:
+        """Largest bond dimension over the instances (synchronises)."""
+        return max(self.info(i)["max_bond"] for i in range(self.n))
+
     def reserve_sites(self, nslots: int):
         nat.check(nat.lib().otb_tempo_reserve_sites(self._h, int(nslots)))
 

@@ -45,3 +45,21 @@ def test_gpu_backends_route_unsupported_reference_features():
                           degeneracy_maps=([0], [0]))
     with pytest.raises(NotImplementedError):
         GpuPtTempoBackend(2, infl, None, np.ones(4), np.zeros(4), 5, 3, 1e-6, {"backend": "gb300"})
+
+
+def test_bucket_tuner_alternates_then_keeps_the_faster_shape():
+    from oqupy_gb300.autotune import BucketTuner
+    t = BucketTuner(candidates=[(256, 56), (512, 200)], bucket_width=8)
+    t.begin_chunk(5)
+    assert t.tuning()
+    shapes = [t.shape_for(k) for k in range(4)]
+    assert shapes == [(256, 56), (512, 200), (256, 56), (512, 200)]
+    t.end_chunk([10.0, 14.0, 11.0, 15.0])           # narrow CTAs faster
+    assert not t.tuning() and t.shape_for(0) == (256, 56)
+    t.begin_chunk(30)                               # a new bucket is tuned again
+    assert t.tuning()
+    t.end_chunk([20.0, 12.0, 21.0, 13.0])
+    assert t.shape_for(3) == (512, 200)
+    t.begin_chunk(6)
+    assert t.shape_for(1) == (256, 56)
+    assert t.table() == {"bond 0-7": [256, 56], "bond 24-31": [512, 200]}
