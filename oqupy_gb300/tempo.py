@@ -232,7 +232,8 @@ class GpuTempoBackend:
     (tempo_backend.py:577-626): same constructor, ``step`` property,
     ``initialize() -> (0, state)`` and ``compute_step() -> (step, state)``.
 
-    ``config`` keys used: ``precision`` ("complex128" | "mixed"), ``chi_cap``
+    ``config`` keys used: ``precision`` ("complex128" | "mixed"), ``block`` /
+    ``smem_kb`` (launch shape, default 512 threads and 200 KiB), ``chi_cap``
     (initial bond capacity; a step whose bonds outgrow it is redone with
     twice the capacity, up to 1152 / D, after replaying the earlier steps on
     a fresh handle -- the engine is deterministic, so the replay repeats
@@ -295,10 +296,13 @@ class GpuTempoBackend:
         if self._batch is not None:
             self._batch.close()
         inst = self._inst
+        # one instance on one CTA: the widest CTA (512 threads) with the
+        # largest shared-memory share
         self._batch = TempoBatch(
             [inst], precision=self._config.get("precision", "complex128"),
             chi_cap=self._cap, out_cap=4, grid=1,
             max_sites=16 if self._dkmax is None else 0,
+            block=int(self._config.get("block", 512)), smem_kb=int(self._config.get("smem_kb", 200)),
             qr_cut=float(self._config.get("qr_cut", 0.0)))
         self._ninfl = len(inst["influences"])
         self._last_props = (inst["prop1"], inst["prop2"])
