@@ -269,15 +269,19 @@ extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const dou
   DevBuf dp1, dp2, drho, dv0, dv1, dout;
   const size_t pb = (size_t)nh * D * D * 16, vb = (size_t)nh * I.cap * D * 16;
   const size_t ob = (size_t)(num_steps + 1) * nh * D * 16;
+  const int max_chunks = (I.cap + 31) / 32;
+  DevBuf dpart, dcnt;
   if (!dp1.alloc(pb) || !dp2.alloc(pb) || !drho.alloc((size_t)nh * D * 16) || !dv0.alloc(vb) ||
-      !dv1.alloc(vb) || !dout.alloc(ob))
+      !dv1.alloc(vb) || !dout.alloc(ob) || !dpart.alloc((size_t)nh * max_chunks * D * 16) ||
+      !dcnt.alloc((size_t)nh * sizeof(unsigned int)))
     return OTB_ERR_OOM;
   cudaStream_t s = (cudaStream_t)stream;
   if (!check_cuda(cudaMemcpyAsync(dp1.p, p1, pb, cudaMemcpyHostToDevice, s), "upload") ||
       !check_cuda(cudaMemcpyAsync(dp2.p, p2, pb, cudaMemcpyHostToDevice, s), "upload") ||
       !check_cuda(cudaMemcpyAsync(drho.p, rho0, (size_t)nh * D * 16, cudaMemcpyHostToDevice, s), "upload") ||
       !check_cuda(cudaMemsetAsync(dout.p, 0, ob, s), "memset") ||
-      !check_cuda(cudaMemsetAsync(dv0.p, 0, vb, s), "memset"))
+      !check_cuda(cudaMemsetAsync(dv0.p, 0, vb, s), "memset") ||
+      !check_cuda(cudaMemsetAsync(dcnt.p, 0, (size_t)nh * sizeof(unsigned int), s), "memset"))
     return OTB_ERR_CUDA;
   DynLaunch L;
   L.nh = nh;
@@ -293,6 +297,9 @@ extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const dou
   L.vcur = (double*)dv0.p;
   L.vnext = (double*)dv1.p;
   L.out = (double*)dout.p;
+  L.partial = (double*)dpart.p;
+  L.counter = (unsigned int*)dcnt.p;
+  L.max_chunks = max_chunks;
   L.k = 0;
   if (!check_cuda(launch_dyn_init(L, (const double*)drho.p, s), "dyn init")) return OTB_ERR_CUDA;
   // the whole sweep as one CUDA graph: one kernel node per step

@@ -11,7 +11,10 @@
 //     rho_h(k+1)[a] = sum_r v'[r][a] cap_{k+1}[r]
 // One launch per step (grid: bond chunks x systems); the host replays the
 // launches of a whole sweep as a CUDA graph.  A transform_in / transform_out
-// of the process tensor is folded into P1 / P2 on the host.
+// of the process tensor is folded into P1 / P2 on the host.  The read-out
+// sum is reproducible bit for bit: a CTA adds its bond chunk's terms in a
+// fixed order, and the last CTA of a system to finish (counted after a
+// memory fence) adds the chunks' partial sums in chunk order.
 #include "common.cuh"
 #include "engine.h"
 
@@ -23,7 +26,7 @@ constexpr int DYN_THREADS = 128;
 
 __global__ void __launch_bounds__(DYN_THREADS) dyn_step_kernel(DynLaunch L) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ double red[2 * 16];
+  __shared__ int last;
   const int h = blockIdx.y;
   const int k = L.k;
   const int D = L.D;
@@ -36,7 +39,6 @@ __global__ void __launch_bounds__(DYN_THREADS) dyn_step_kernel(DynLaunch L) {
   const zc* v = (const zc*)L.vcur + (long long)h * L.cap * D;
   const zc* P1 = (const zc*)L.p1 + (long long)h * D * D;
   const zc* P2 = (const zc*)L.p2 + (long long)h * D * D;
-  if (tid < 2 * D) red[tid] = 0.0;
   for (int idx = tid; idx < l * D; idx += nt) {
     const int ll = idx / D, a = idx - ll * D;
     zc acc = mk<double>(0, 0);
@@ -55,19 +57,36 @@ __global__ void __launch_bounds__(DYN_THREADS) dyn_step_kernel(DynLaunch L) {
   __syncthreads();
   zc* vn = (zc*)L.vnext + (long long)h * L.cap * D;
   const zc* capn = (const zc*)L.caps + (long long)(k + 1) * L.cap;
+  zc* cb = w + DYN_RB * D;   // read-out terms of this chunk, [rr][a]
   for (int idx = tid; idx < rn * D; idx += nt) {
     const int rr = idx / D, a = idx - rr * D;
     zc y = mk<double>(0, 0);
     for (int b = 0; b < D; ++b) cfma(y, P2[a * D + b], w[rr * D + b]);
     vn[(size_t)(r0 + rr) * D + a] = y;
-    const zc c = cmul(y, capn[r0 + rr]);
-    atomicAdd(&red[2 * a], c.x);
-    atomicAdd(&red[2 * a + 1], c.y);
+    cb[idx] = cmul(y, capn[r0 + rr]);
   }
   __syncthreads();
-  if (tid < 2 * D) {
-    double* out = L.out + 2 * ((long long)(k + 1) * L.nh * D + (long long)h * D);
-    atomicAdd(out + tid, red[tid]);
+  zc* part = (zc*)L.partial + (long long)h * L.max_chunks * D;
+  if (tid < D) {
+    zc acc = mk<double>(0, 0);
+    for (int rr = 0; rr < rn; ++rr) acc = acc + cb[rr * D + tid];
+    part[blockIdx.x * D + tid] = acc;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last = (atomicAdd(L.counter + h, 1u) == gridDim.x - 1) ? 1 : 0;
+  __syncthreads();
+  if (last) {
+    if (tid < D) {
+      zc acc = mk<double>(0, 0);
+      for (int c = 0; c < (int)gridDim.x; ++c) {
+        const double2 q = __ldcg(reinterpret_cast<const double2*>(part + c * D + tid));
+        acc = acc + mk<double>(q.x, q.y);
+      }
+      zc* out = (zc*)L.out + (long long)(k + 1) * L.nh * D + (long long)h * D;
+      out[tid] = acc;
+    }
+    if (tid == 0) L.counter[h] = 0u;
   }
 }
 
@@ -88,7 +107,7 @@ __global__ void dyn_init_kernel(DynLaunch L, const double* rho0) {
 
 cudaError_t launch_dyn_step(const DynLaunch& L, int r, cudaStream_t stream) {
   const int chunks = (r + DYN_RB - 1) / DYN_RB;
-  const size_t smem = (size_t)(L.cap * L.D + DYN_RB * L.D) * sizeof(zc);
+  const size_t smem = (size_t)(L.cap * L.D + 2 * DYN_RB * L.D) * sizeof(zc);
   dim3 grid(chunks, L.nh);
   dyn_step_kernel<<<grid, DYN_THREADS, smem, stream>>>(L);
   return cudaGetLastError();

@@ -139,6 +139,9 @@ struct DynLaunch {
   double* vcur;         // nh * cap * D
   double* vnext;
   double* out;          // (num_steps + 1) * nh * D
+  double* partial;      // nh * max_chunks * D complex: per-chunk read-out sums
+  unsigned int* counter;  // nh counters of finished chunks (zero between steps)
+  int max_chunks;
   int k;                // step
 };
 
