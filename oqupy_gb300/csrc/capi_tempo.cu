@@ -234,6 +234,17 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     const InstDev& I = h->inst[i];
     const int D = I.D;
     std::vector<double> r0(ins[i].rho0, ins[i].rho0 + 2 * D);
+    if (h->precision == OTB_PRECISION_MIXED) {
+      // the mixed form's sites are double-float: each double x stored as the
+      // float pair (hi, lo) with hi + lo = x to 48 bits
+      std::vector<float> ffv(4 * D);
+      for (int q = 0; q < 2 * D; ++q) {
+        const float hi = (float)r0[q];
+        ffv[2 * q] = hi;
+        ffv[2 * q + 1] = (float)(r0[q] - (double)hi);
+      }
+      std::memcpy(r0.data(), ffv.data(), ffv.size() * sizeof(float));
+    }
     if (!check_cuda(cudaMemcpy((char*)h->d_sites.p + I.site_base * h->elem, r0.data(),
                                r0.size() * sizeof(double), cudaMemcpyHostToDevice),
                     "init site"))

@@ -138,6 +138,41 @@ __device__ __forceinline__ void ccacc_fmaj(ccacc& acc, const cff& a, const cff& 
   ffp_acc(-a.y.hi, -a.y.lo, b.x.hi, b.x.lo, acc.yh, acc.yl);
 }
 
+// The accumulated value as a double-float complex (no FP64 instruction).
+__device__ __forceinline__ cff ccacc_cff(const ccacc& a) {
+  cff r;
+  r.x = two_sum(a.xh, a.xl);
+  r.y = two_sum(a.yh, a.yl);
+  return r;
+}
+
+__device__ __forceinline__ cff cff_add(const cff& a, const cff& b) {
+  cff r;
+  r.x = ff_add(a.x, b.x);
+  r.y = ff_add(a.y, b.y);
+  return r;
+}
+
+// a * s for a real double-float s
+__device__ __forceinline__ cff cff_scale(const cff& a, ff s) {
+  cff r;
+  r.x = ff_mul(a.x, s);
+  r.y = ff_mul(a.y, s);
+  return r;
+}
+
+__device__ __forceinline__ cff cff_conj(cff a) {
+  a.y.hi = -a.y.hi;
+  a.y.lo = -a.y.lo;
+  return a;
+}
+
+__device__ __forceinline__ cff cff_mul(const cff& a, const cff& b) {
+  ccacc f = ccacc_zero();
+  ccacc_fma(f, a, b);
+  return ccacc_cff(f);
+}
+
 __device__ __forceinline__ cx<double> ccacc_value(const ccacc& a) {
   return mk<double>((double)a.xh + (double)a.xl, (double)a.yh + (double)a.yl);
 }

@@ -377,6 +377,9 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
   return sweep;
 }
 
+__device__ inline int jacobi_rank(int n, double epsrel, double* norm, int* perm, JacobiShared* sh,
+                                  int sweeps, double tail2);
+
 // FP64 column norms of W, descending order and the kept rank (>= 1).
 template <typename T>
 __device__ int jacobi_finish(const cx<T>* W, int m, int n, int ld, double epsrel, double* norm,
@@ -395,6 +398,15 @@ __device__ int jacobi_finish(const cx<T>* W, int m, int n, int ld, double epsrel
     if (l == 0) norm[j] = sqrt(acc);
   }
   __syncthreads();
+  return jacobi_rank(n, epsrel, norm, perm, sh, sweeps, tail2);
+}
+
+// Descending order of the n values norm[] and the kept rank (>= 1): the
+// second half of jacobi_finish, for callers that computed the norms.
+__device__ inline int jacobi_rank(int n, double epsrel, double* norm, int* perm, JacobiShared* sh,
+                                  int sweeps, double tail2) {
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
   for (int j = tid; j < n; j += nthreads) {
     const double sj = norm[j];
     int rank = 0;

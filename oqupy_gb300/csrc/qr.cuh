@@ -567,4 +567,132 @@ __device__ int qr_jacobi_truncate(cx<double>* W, int R, int N, typename QA<T>::E
   return kk;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float input and output (the mixed form's TEMPO step keeps sites,
+// carries and theta in double-float): no FP64 instruction per matrix element.
+// ---------------------------------------------------------------------------
+
+// x * 2^e for a double-float complex x: exact (two float multiplications by
+// a power of two) unless it leaves the float range.
+__device__ __forceinline__ cff cff_ldexp(cff x, float p2) {
+  x.x.hi *= p2;
+  x.x.lo *= p2;
+  x.y.hi *= p2;
+  x.y.lo *= p2;
+  return x;
+}
+
+// FP64 norms of the n columns of W (m rows, ld), accumulated in double-float.
+__device__ inline void cff_column_norms(const cff* W, int m, int n, int ld, double* norm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int j = tid / 32; j < n; j += nt / 32) {
+    const int l = tid & 31;
+    ff acc = ff_make(0.f, 0.f);
+    const cff* c = W + (size_t)j * ld;
+    for (int r = l; r < m; r += 32) acc = ff_fma(c[r].x, c[r].x, ff_fma(c[r].y, c[r].y, acc));
+    for (int off = 16; off > 0; off >>= 1) acc = ff_add(acc, ff_shfl_xor(acc, off));
+    if (l == 0) norm[j] = ff_to(ff_sqrt(acc));
+  }
+  __syncthreads();
+}
+
+// FP64 sweeps on a double-float matrix whose double-float sweeps did not
+// settle: converted in place (both 16-byte elements), swept, converted back.
+__device__ inline int cff_fp64_fallback(cff* W, int m, int n, int ld, JacobiShared* sh) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  cx<double>* Wd = reinterpret_cast<cx<double>*>(W);
+  for (int j = 0; j < n; ++j)
+    for (int r = tid; r < m; r += nt) {
+      const size_t q = (size_t)j * ld + r;
+      Wd[q] = cff_to(W[q]);
+    }
+  __syncthreads();
+  const int sw = jacobi_sweeps<double>(Wd, m, n, ld, nullptr, 0, sh);
+  for (int j = 0; j < n; ++j)
+    for (int r = tid; r < m; r += nt) {
+      const size_t q = (size_t)j * ld + r;
+      W[q] = cff_from(Wd[q]);
+    }
+  __syncthreads();
+  return sw;
+}
+
+// The split driver on a double-float input already in X (R x N, ld R,
+// scaled by 1 / scale, a power of two), with Zbuf (R x N) as spare global
+// storage and zs / zs_bytes spare shared memory.  Returns the kept rank;
+// *Wout (double-float, N x kk or N x k, ld N, in original units) holds
+// V_A Sigma with norm / perm as in jacobi_finish (the k <= N / 2 branch
+// stores its kept columns sorted, perm the identity).
+__device__ inline int qr_jacobi_truncate_ff(cff* X, int R, int N, double scale, cff* Zbuf, unsigned char* zs,
+                                            size_t zs_bytes, double epsrel, float delta, double* norm,
+                                            int* perm, JacobiShared* sh, cff** Wout) {
+  typedef QA<ff> Q;
+  const int tid = threadIdx.x;
+  const int nt = blockDim.x;
+  const float up = (float)scale;    // power of two in float range for the data this path sees
+  float* cn = reinterpret_cast<float*>(norm);
+  if (!(delta > 0.f)) delta = qr_default_delta(true, epsrel);
+  float tail2;
+  const int k = qrcp_inplace<ff>(X, R, N, delta, cn, reinterpret_cast<short*>(perm), &tail2);
+  const int* colstep = reinterpret_cast<const int*>(norm);
+  cff* Z = ((size_t)N * k * sizeof(cff) <= zs_bytes) ? reinterpret_cast<cff*>(zs) : Zbuf;
+  for (int idx = tid; idx < N * k; idx += nt) {
+    const int i = idx / N, q = idx - i * N;
+    Z[idx] = (colstep[q] >= i) ? Q::conj(X[(size_t)q * R + i]) : Q::zeroE();
+  }
+  __syncthreads();
+  const double t2 = (double)tail2 * scale * scale;
+  if (k >= 8 && 2 * k <= N) {
+    // second QR, Jacobi on the k x k R2, kept columns transformed back
+    // (as in qr_jacobi_truncate)
+    cff* R2 = X + (size_t)N * k;
+    double* tau = reinterpret_cast<double*>(X + (size_t)N * k + (size_t)k * k);
+    householder_unit<ff>(Z, N, k, N, tau);
+    for (int idx = tid; idx < k * k; idx += nt) {
+      const int c = idx / k, r = idx - c * k;
+      R2[idx] = (r <= c) ? Z[(size_t)c * N + r] : Q::zeroE();
+    }
+    __syncthreads();
+    const int sw = jacobi_sweeps_ff(R2, k, k, k, sh);
+    int sw64 = 0;
+    if (!(sw < JACOBI_MAX_SWEEPS || sh->noise_converged)) sw64 = cff_fp64_fallback(R2, k, k, k, sh);
+    if (tid == 0) sh->sweeps32 = sw;
+    cff_column_norms(R2, k, k, k, norm);
+    for (int j = tid; j < k; j += nt) norm[j] *= scale;
+    __syncthreads();
+    const int kk = jacobi_rank(k, epsrel, norm, perm, sh, sw64, t2);
+    if (tid == 0) sh->sweeps = sw64;
+    cff* Y = X;
+    for (int idx = tid; idx < N * kk; idx += nt) {
+      const int j = idx / N, r = idx - j * N;
+      Y[idx] = (r < k) ? R2[(size_t)perm[j] * k + r] : Q::zeroE();
+    }
+    __syncthreads();
+    apply_q_unit<ff>(Z, N, k, N, tau, Y, kk, N);
+    for (int idx = tid; idx < N * kk; idx += nt) Y[idx] = cff_ldexp(Y[idx], up);
+    for (int j = tid; j < kk; j += nt) tau[j] = norm[perm[j]];
+    __syncthreads();
+    for (int j = tid; j < kk; j += nt) {
+      norm[j] = tau[j];
+      perm[j] = j;
+    }
+    __syncthreads();
+    *Wout = Y;
+    return kk;
+  }
+  const int sw = jacobi_sweeps_ff(Z, N, k, N, sh);
+  int sw64 = 0;
+  if (!(sw < JACOBI_MAX_SWEEPS || sh->noise_converged)) sw64 = cff_fp64_fallback(Z, N, k, N, sh);
+  if (tid == 0) sh->sweeps32 = sw;
+  cff_column_norms(Z, N, k, N, norm);
+  for (int j = tid; j < k; j += nt) norm[j] *= scale;
+  __syncthreads();
+  const int kk = jacobi_rank(k, epsrel, norm, perm, sh, sw64, t2);
+  if (tid == 0) sh->sweeps = sw64;
+  for (int idx = tid; idx < N * k; idx += nt) Z[idx] = cff_ldexp(Z[idx], up);
+  __syncthreads();
+  *Wout = Z;
+  return kk;
+}
+
 }  // namespace otb

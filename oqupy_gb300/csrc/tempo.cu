@@ -65,6 +65,7 @@ struct SharedStep {
   JacobiShared jsh;
   double norm[NMAX];
   int perm[NMAX];
+  cff pf[3][81];   // mixed form: P1, P2 and the site's influence in double-float
   int inst;
 };
 
@@ -122,6 +123,12 @@ __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R,
   *Wout = W;
   return kk;
 }
+
+}  // namespace otb
+
+#include "tempo_ff.cuh"
+
+namespace otb {
 
 template <bool MIXED>
 __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& b,
@@ -577,7 +584,10 @@ __global__ void __launch_bounds__(TEMPO_THREADS, 1) tempo_kernel(TempoLaunch L) 
     const int i = L.order[q];
     const InstDev I = L.inst[i];
     for (int s = 0; s < L.nsteps; ++s) {
-      tempo_step<MIXED>(L, I, i, b, sh);
+      if (MIXED)
+        tempo_step_ff(L, I, i, b, sh);
+      else
+        tempo_step<false>(L, I, i, b, sh);
       __syncthreads();
       if (sh.st.status != ST_OK) break;
     }
@@ -650,7 +660,13 @@ __global__ void __launch_bounds__(STATIC_THREADS)
   __syncthreads();
   if (sh.st.step == 0 && sh.st.nsites == 0) {
     // first call on a zeroed MPS buffer: the initial state as a (1, D, 1) site
-    for (int a = tid; a < I.D; a += blockDim.x) b.sites[a] = ((const zc*)rho0)[a];
+    // the mixed form keeps its sites in double-float
+    for (int a = tid; a < I.D; a += blockDim.x) {
+      if (MIXED)
+        reinterpret_cast<cff*>(b.sites)[a] = cff_from(((const zc*)rho0)[a]);
+      else
+        b.sites[a] = ((const zc*)rho0)[a];
+    }
     if (tid == 0) {
       b.dims[0] = make_int2(1, 1);
       sh.st.nsites = 1;
@@ -664,7 +680,10 @@ __global__ void __launch_bounds__(STATIC_THREADS)
   const int first = sh.st.step;
   __syncthreads();
   for (int s = 0; s < nsteps; ++s) {
-    tempo_step<MIXED>(L, I, 0, b, sh);
+    if (MIXED)
+      tempo_step_ff(L, I, 0, b, sh);
+    else
+      tempo_step<false>(L, I, 0, b, sh);
     __syncthreads();
     if (sh.st.status != ST_OK) break;
   }
