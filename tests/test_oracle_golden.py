@@ -90,3 +90,24 @@ def test_bath_oracle_influences_match_reference(name):
                                   g["add_corr"], g["epsrel"])
         np.testing.assert_allclose(got, g["tempo_infl"][dk], rtol=0,
                                    atol=1e-13)
+
+
+def test_oracle_reproduces_the_batched_draw_fixtures():
+    """The draws fixtures (tests/golden/make_draws.py) are the oracle's own
+    states on their stored inputs: two spin-boson and one qutrit draw,
+    rerun for their first steps, agree to rounding."""
+    import os
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    for kind, idx, steps in (("spin_boson", [0, 7], 25), ("qutrit", [3], 6)):
+        g = np.load(os.path.join(d, f"draws_{kind}.npz"))
+        for i in idx:
+            infl = g["influences"][i]
+            nan = np.full_like(infl[0], np.nan)     # dk past the stored window: never used
+
+            def influence(dk, infl=infl, nan=nan):
+                return None if dk < 0 else (infl[dk] if dk < len(infl) else nan)
+            st, _ = to.tempo_dynamics(g["rho0"][i].reshape(-1), influence,
+                                      g["unitary"][i], lambda s: (g["prop1"][i], g["prop2"][i]),
+                                      int(g["dkmax"][i]), float(g["epsrel"][i]), steps)
+            err = max(to.trace_distance(a, b) for a, b in zip(st, g["states"][i][: steps + 1]))
+            assert err <= 1e-12 + 10 * g["env14"][i][: steps + 1].max(), (kind, i, err)
