@@ -105,3 +105,38 @@ def test_device_baseline_matches_host_precession():
     nat.check(nat.lib().otb_mlp_bloch_free_add(y.data_ptr(), oe.data_ptr(), len(P), nsteps, dt, None))
     got = y.cpu().numpy().reshape(len(P), 3, nsteps)
     np.testing.assert_allclose(got, free_bloch(P, nsteps, dt), atol=2e-5)
+
+
+def test_screening_gain_over_tempo_only():
+    """What the trained network gains over TEMPO-only screening of the same
+    points: at a budget met by part of the box (the calibrated error of the
+    two best of four alpha x T regions), the points answered by the network
+    skip their TEMPO solve.  Points/s of screening with fallback against
+    TEMPO alone, and the error after fallback against the direct solve."""
+    import time
+    from oqupy_gb300.surrogate import Surrogate, sample_params, tempo_bloch
+    nsteps = 60
+    sur = Surrogate(nsteps=nsteps, hidden=(256, 256, 256), dkmax=5, bins=2, seed=1)
+    Ptr = sample_params(768, 10)
+    Ytr, _ = tempo_bloch(Ptr, nsteps, dkmax=5)
+    Pva = sample_params(256, 11)
+    Yva, _ = tempo_bloch(Pva, nsteps, dkmax=5)
+    sur.fit(Ptr, Ytr, epochs=60, batch=128, lr=2e-3)
+    sur.calibrate(Pva, Yva)
+    budget = float(np.sort(sur.err_map)[1])
+    Pte = sample_params(512, 13)
+    tempo_bloch(Pte[:8], nsteps, dkmax=5)                 # warm-up
+    t0 = time.perf_counter()
+    ref, _ = tempo_bloch(Pte, nsteps, dkmax=5)
+    t_tempo = time.perf_counter() - t0
+    sur.screen(Pte[:8], budget=budget)                    # warm-up
+    out, fb, tim = sur.screen(Pte, budget=budget)
+    gain = tim["points_per_s"] / (len(Pte) / t_tempo)
+    err = np.abs(out - ref).max(axis=(1, 2))
+    print(f"budget {budget:.2e}: network answers {(~fb).mean():.0%} of the points, "
+          f"{tim['points_per_s']:.0f} vs {len(Pte) / t_tempo:.0f} points/s TEMPO-only "
+          f"(gain {gain:.2f}x); error after fallback p90 {np.quantile(err, 0.9):.2e}, "
+          f"max {err.max():.2e}")
+    assert (~fb).mean() > 0.2
+    assert gain > 1.0
+    assert np.quantile(err, 0.9) <= 2.0 * budget
