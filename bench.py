@@ -709,7 +709,7 @@ def run_tempo(args, rank, world):
     from oqupy_gb300 import TempoBatch, _native
     from oqupy_gb300 import multigpu as mg
     dev_stream = torch.cuda.current_stream()
-    shape = dict(chi_cap=args.chi_cap, qr_cut=args.qr_cut, block=args.block, smem_kb=args.smem_kb)
+    batch_kw = dict(chi_cap=args.chi_cap, qr_cut=args.qr_cut, block=args.block, smem_kb=args.smem_kb)
     t_setup = time.perf_counter()
     insts = make_instances(args.instances, BATCH_SEED)
     setup_s = time.perf_counter() - t_setup       # influences + propagators on the host
@@ -723,7 +723,7 @@ def run_tempo(args, rank, world):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # warm-up: W bench steps of a separate batch
     warm = TempoBatch(make_instances(len(local), BATCH_SEED + 7919), precision="mixed",
-                      out_cap=2, **shape)
+                      out_cap=2, **batch_kw)
     for _ in range(args.warmup):
         warm.advance(CHUNK, dev_stream.cuda_stream)
     torch.cuda.synchronize()
@@ -745,7 +745,7 @@ def run_tempo(args, rank, world):
     barrier()
     clocks.start()
     t0 = time.perf_counter()
-    b = TempoBatch(local, precision="mixed", out_cap=CHUNK + 1, **shape)
+    b = TempoBatch(local, precision="mixed", out_cap=CHUNK + 1, **batch_kw)
     h2d = sum(np.asarray(x["influences"]).nbytes + np.asarray(x["prop1"]).nbytes
               + np.asarray(x["prop2"]).nbytes + np.asarray(x["rho0"]).nbytes for x in local)
     d2h = 0
@@ -758,11 +758,11 @@ def run_tempo(args, rank, world):
         flush.zero_()
         if tuner is not None:
             tuner.begin_chunk(b.max_bond() if done else 1)
-        shape = None
+        cur = None
         for j in range(n):
-            if tuner is not None and tuner.shape_for(j) != shape:
-                shape = tuner.shape_for(j)
-                b.set_launch(shape[0], shape[1])
+            if tuner is not None and tuner.shape_for(j) != cur:
+                cur = tuner.shape_for(j)
+                b.set_launch(cur[0], cur[1])
             ev[done + j][0].record(dev_stream)
             b.advance(1, dev_stream.cuda_stream)
             ev[done + j][1].record(dev_stream)
@@ -791,7 +791,7 @@ def run_tempo(args, rank, world):
     c128 = None
     nc = min(args.c128_steps, done)
     if nc > 0 and not args.no_complex128:
-        bc = TempoBatch(local, precision="complex128", out_cap=nc + 1, **shape)
+        bc = TempoBatch(local, precision="complex128", out_cap=nc + 1, **batch_kw)
         evc = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(nc)]
         torch.cuda.synchronize()

@@ -157,7 +157,8 @@ typedef struct {
   int32_t precision;   /* OTB_PRECISION_* */
   int32_t chi_cap;     /* bond-dimension capacity of every site, chi_cap * D <= 1152 */
   int32_t grid;        /* CTAs per launch, 0 = 2 per SM */
-  double qr_cut;       /* as otb_tempo_config.qr_cut (0 = default) */
+  double qr_cut;       /* as otb_tempo_config.qr_cut; 0 = default: 1e-14
+                          (complex128), min(1e-3 epsrel, 1e-11) (mixed) */
 } otb_pt_config;
 
 typedef struct {
