@@ -688,6 +688,17 @@ def _accuracy_vs_oracle(states, indices):
                               "oracle_envelope_max": r[3]} for r in rows]}
 
 
+def tempo_workload_config(n, timed_steps):
+    """The batched spin-boson workload's ``config`` (identical in both arms)."""
+    return {"workload": (f"batched TEMPO spin-boson, {n} instances (alpha U[0.01,0.5], "
+                         "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
+                         "epsrel 1e-6), whole 500-step trajectories"),
+            "instances": n, "seed": BATCH_SEED,
+            "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
+            "timed_steps": f"1..{timed_steps} of {NSTEPS_TRAJ}",
+            "l2": "GPU arm: flushed (256 MiB write) before every bench step; site rings >> L2"}
+
+
 def run_tempo(args, rank, world):
     """The headline workload: whole 500-step trajectories of the batch.
 
@@ -817,6 +828,18 @@ def run_tempo(args, rank, world):
                     "frac_le_1e-6": float(np.mean(td <= 1e-6))},
                 "complex128_sweeps64_per_split": sum(x["sweeps64"] for x in ic) / max(1, sum(x["splits"] for x in ic))}
 
+    # the last launch's timeline (device clock per instance): is a late step
+    # bound by its longest instance or by the sum of all instances' work?
+    tb = np.array([x["t_begin_ns"] for x in infos], dtype=np.int64)
+    te = np.array([x["t_end_ns"] for x in infos], dtype=np.int64)
+    dur = (te - tb) / 1e6
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    timeline = {"step": done, "launch_ms": float((te.max() - tb.min()) / 1e6),
+                "longest_instance_ms": float(dur.max()),
+                "instance_ms_sum_over_sms": float(dur.sum() / sms),
+                "instance_ms_p50": float(np.median(dur)), "sms": int(sms),
+                "note": ("per-instance device-clock span in the last launch: launch_ms close to "
+                         "longest_instance_ms means the step waits on one instance's split chain")}
     nsplit = max(1, sum(x["splits"] for x in infos))
     stats = {"max_bond": max(x["max_bond"] for x in infos), "splits": nsplit,
              "sweeps64_per_split": sum(x["sweeps64"] for x in infos) / nsplit,
@@ -844,17 +867,11 @@ def run_tempo(args, rank, world):
             "higher_is_better": True, "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "c128 storage; splits and contractions in double-float (f32 pairs)",
             "data": "synthetic (seeded draws of the batched spin-boson distribution)",
-            "config": {"workload": (f"batched TEMPO spin-boson, {len(insts)} instances (alpha U[0.01,0.5], "
-                                    "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
-                                    "epsrel 1e-6), whole 500-step trajectories"),
-                       "instances": len(insts), "seed": BATCH_SEED,
-                       "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
-                       "timed_steps": f"1..{done} of {NSTEPS_TRAJ}",
-                       "warmup": f"{args.warmup} bench steps on a separate batch (seed {BATCH_SEED + 7919})",
-                       "l2": "flushed (256 MiB write) before every bench step; site rings >> L2",
-                       "precision": "mixed", "parallelism": f"instances x {world} GPUs",
-                       "launch": ({"autotuned_per_bond_bucket": tuner.table()} if tuner is not None
-                                  else {"block": args.block or 256, "smem_kb": args.smem_kb or 56})},
+            "config": tempo_workload_config(len(insts), done),
+            "arm": {"precision": "mixed", "parallelism": f"instances x {world} GPUs",
+                    "warmup": f"{args.warmup} bench steps on a separate batch (seed {BATCH_SEED + 7919})",
+                    "launch": ({"autotuned_per_bond_bucket": tuner.table()} if tuner is not None
+                               else {"block": args.block or 256, "smem_kb": args.smem_kb or 56})},
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": len(insts) * frac_traj / e2e_all, "unit": "trajectories/s",
                     "h2d_bytes_per_step": int(h2d // max(1, args.steps)),
@@ -862,6 +879,7 @@ def run_tempo(args, rank, world):
                     "note": ("same run, wall clock: handle creation from host arrays (all inputs "
                              "host->device), every launch, every bench step's states device->host")},
             "clocks": clk, "gpu_launches": int(done), "mixed_stats": stats,
+            "last_launch_timeline": timeline,
             "setup_seconds": setup_s,
             "ms_per_step_by_block": [float(ms[i:i + 50].sum()) / len(ms[i:i + 50]) for i in range(0, done, 50)],
             "accuracy_vs_fp64_oracle": acc}
@@ -887,14 +905,9 @@ def run_reference(args, rank, world):
             "ms_per_step": 1e3 * args.instances / value / NSTEPS_TRAJ * CHUNK,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic (seeded draws of the batched spin-boson distribution)",
-            "config": {"workload": (f"batched TEMPO spin-boson, {args.instances} instances (alpha U[0.01,0.5], "
-                                    "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
-                                    "epsrel 1e-6), whole 500-step trajectories"),
-                       "instances": args.instances, "seed": BATCH_SEED,
-                       "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
-                       "timed_steps": f"1..{min(args.steps * CHUNK, NSTEPS_TRAJ)} of {NSTEPS_TRAJ}",
-                       "warmup": "none (CPU)", "l2": "n/a (CPU)",
-                       "precision": "complex128", "parallelism": f"one single-threaded process per core x {procs}"},
+            "config": tempo_workload_config(args.instances, min(args.steps * CHUNK, NSTEPS_TRAJ)),
+            "arm": {"precision": "complex128", "parallelism": f"one single-threaded process per core x {procs}",
+                    "warmup": "none (CPU)"},
             "impl": "reference",
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": value, "unit": "trajectories/s", "h2d_bytes_per_step": 0,

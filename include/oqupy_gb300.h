@@ -97,6 +97,10 @@ typedef struct {
   double flops_alg;   /* algorithmic flops done so far: per split of a complex
                          R x N matrix (R >= N) 4 (6 R N^2 + 20 N^3), plus
                          8 flops per complex multiply-add of the contractions */
+  int64_t t_begin_ns; /* device clock (ns, %globaltimer) at which the last
+                         launch's CTA took this instance, */
+  int64_t t_end_ns;   /* ... and at which it finished the launch's steps:
+                         the launch's timeline, for critical-path analysis */
 } otb_tempo_info;
 
 /* Replaces TempoBackend.__init__ + initialize (tempo_backend.py:583-617). */

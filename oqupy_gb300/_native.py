@@ -61,7 +61,8 @@ class TempoInfo(ctypes.Structure):
                 ("nsites", ctypes.c_int32), ("max_bond", ctypes.c_int32),
                 ("log_scale", ctypes.c_double), ("splits", ctypes.c_int32),
                 ("sweeps64", ctypes.c_int32), ("sweeps32", ctypes.c_int32),
-                ("flops_alg", ctypes.c_double)]
+                ("flops_alg", ctypes.c_double), ("t_begin_ns", ctypes.c_int64),
+                ("t_end_ns", ctypes.c_int64)]
 
 
 class PtConfig(ctypes.Structure):

@@ -205,6 +205,8 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
     st.sweeps64 = 0;
     st.sweeps32 = 0;
     st.flops_alg = 0.0;
+    st.t_begin_ns = 0;
+    st.t_end_ns = 0;
   }
   long long out_total = 0;
   for (int i = 0; i < n; ++i) {
@@ -366,6 +368,8 @@ extern "C" otb_status otb_tempo_get_info(otb_tempo* h, int32_t inst, otb_tempo_i
   info->sweeps64 = s.sweeps64;
   info->sweeps32 = s.sweeps32;
   info->flops_alg = s.flops_alg;
+  info->t_begin_ns = s.t_begin_ns;
+  info->t_end_ns = s.t_end_ns;
   return OTB_OK;
 }
 

@@ -38,6 +38,8 @@ struct InstState {
   int sweeps64;    // FP64 Jacobi sweeps done so far
   int sweeps32;    // double-float Jacobi sweeps done so far (mixed form)
   double flops_alg;  // algorithmic flops done so far (R-SVD count + contractions)
+  long long t_begin_ns;  // device clock (globaltimer) when the last launch took this instance
+  long long t_end_ns;    // ... and when it finished its steps
 };
 
 struct TempoLaunch {

@@ -78,6 +78,13 @@ struct SharedStep {
 // matrices that fit.
 constexpr int QR_MIN_COLS = 8;
 
+// Device clock in ns (the launch timeline recorded per instance).
+__device__ __forceinline__ long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return (long long)t;
+}
+
 template <bool MIXED>
 __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel, float qr_delta,
                      Bufs& b, SharedStep& sh, zc** Wout, bool* flip) {
@@ -583,6 +590,7 @@ __global__ void __launch_bounds__(TEMPO_THREADS, 1) tempo_kernel(TempoLaunch L) 
     if (q >= L.n) break;
     const int i = L.order[q];
     const InstDev I = L.inst[i];
+    const long long t0 = globaltimer_ns();
     for (int s = 0; s < L.nsteps; ++s) {
       if (MIXED)
         tempo_step_ff(L, I, i, b, sh);
@@ -590,6 +598,10 @@ __global__ void __launch_bounds__(TEMPO_THREADS, 1) tempo_kernel(TempoLaunch L) 
         tempo_step<false>(L, I, i, b, sh);
       __syncthreads();
       if (sh.st.status != ST_OK) break;
+    }
+    if (threadIdx.x == 0) {
+      L.state[i].t_begin_ns = t0;
+      L.state[i].t_end_ns = globaltimer_ns();
     }
   }
 }
@@ -746,6 +758,7 @@ extern "C" otb_status otb_tempo_advance_static(const otb_tempo_static_io* io, in
   TempoLaunch L;
   L.n = 1;
   L.inst = nullptr;
+  static_assert(sizeof(InstState) <= 256, "state header of the static MPS buffer");
   L.state = (InstState*)mps;
   L.dims = (int2*)(mps + 256);
   L.sites = mps + 256 + (((size_t)nslots * sizeof(int2) + 255) / 256) * 256;

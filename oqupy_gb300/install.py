@@ -9,6 +9,10 @@ class otherwise, so existing code selects the GPU path through its existing
 configuration.  The factory dispatches before the reference constructor runs,
 so the reference never sees the unknown backend name.
 
+``oqupy.MeanFieldTempo`` builds ``MeanFieldTempoBackend(..., config=...)``
+(oqupy/tempo.py:818-832), rebound the same way to ``mean_field.py``'s
+batched backend.
+
 ``PtTempo.get_process_tensor`` (oqupy/pt_tempo.py:280-306) returns, for a
 GPU build, a ``DeviceProcessTensor`` (``device_pt.py``): a
 ``BaseProcessTensor`` whose tensors stay in device memory.
@@ -56,6 +60,25 @@ def install(oqupy_module: Any = None) -> None:
 
         tempo_backend.reference_class = ref_cls
         tempo_mod.TempoBackend = tempo_backend
+
+    if "MeanFieldTempoBackend" not in _installed:
+        # oqupy.MeanFieldTempo builds MeanFieldTempoBackend(..., config=...,
+        # degeneracy_maps_list=...) (oqupy/tempo.py:818-832)
+        from .mean_field import GpuMeanFieldTempoBackend
+        ref_mf = tempo_mod.MeanFieldTempoBackend
+        _installed["MeanFieldTempoBackend"] = ref_mf
+
+        def mean_field_backend(*args, config=None, degeneracy_maps_list=None, **kwargs):
+            plain = degeneracy_maps_list is None or all(m is None for m in degeneracy_maps_list)
+            if _wants_gpu(config) and plain:
+                return GpuMeanFieldTempoBackend(*args, config=config,
+                                                degeneracy_maps_list=None, **kwargs)
+            if _wants_gpu(config):
+                config = {k: v for k, v in config.items() if k != "backend"}
+            return ref_mf(*args, config=config, degeneracy_maps_list=degeneracy_maps_list, **kwargs)
+
+        mean_field_backend.reference_class = ref_mf
+        tempo_mod.MeanFieldTempoBackend = mean_field_backend
 
     pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
     from .pt import GpuPtTempoBackend
@@ -153,6 +176,8 @@ def uninstall(oqupy_module: Any = None) -> None:
     tempo_mod = importlib.import_module(oqupy_module.__name__ + ".tempo")
     if "TempoBackend" in _installed:
         tempo_mod.TempoBackend = _installed.pop("TempoBackend")
+    if "MeanFieldTempoBackend" in _installed:
+        tempo_mod.MeanFieldTempoBackend = _installed.pop("MeanFieldTempoBackend")
     pt_mod = importlib.import_module(oqupy_module.__name__ + ".pt_tempo")
     if "PtTempoBackend" in _installed:
         pt_mod.PtTempoBackend = _installed.pop("PtTempoBackend")

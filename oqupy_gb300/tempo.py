@@ -142,7 +142,18 @@ class TempoBatch:
         return {"step": inf.step, "status": inf.status, "nsites": inf.nsites,
                 "max_bond": inf.max_bond, "log_scale": inf.log_scale,
                 "splits": inf.splits, "sweeps64": inf.sweeps64,
-                "sweeps32": inf.sweeps32, "flops_alg": inf.flops_alg}
+                "sweeps32": inf.sweeps32, "flops_alg": inf.flops_alg,
+                "t_begin_ns": inf.t_begin_ns, "t_end_ns": inf.t_end_ns}
+
+    def timeline(self) -> np.ndarray:
+        """(n, 2) device-clock ns at which the last launch's CTA took each
+        instance and finished it: the launch's critical path is the instance
+        that ends last, its load balance the spread of the end times."""
+        out = np.zeros((self.n, 2), dtype=np.int64)
+        for i in range(self.n):
+            inf = self.info(i)
+            out[i] = (inf["t_begin_ns"], inf["t_end_ns"])
+        return out
 
     def check_status(self):
         for i in range(self.n):

@@ -20,6 +20,7 @@ Reference being restated (OQuPy 0.5.0, paths relative to the project root):
 * ``oqupy/backends/node_array.py:301-411``  ``NodeArray.contract`` (trace-out)
 * ``oqupy/backends/tempo_backend.py:379-575`` ``BaseTempoBackend``
 * ``oqupy/backends/tempo_backend.py:610-626`` ``TempoBackend.initialize/compute_step``
+* ``oqupy/backends/tempo_backend.py:629-773`` ``MeanFieldTempoBackend``
 * ``oqupy/backends/pt_tempo_backend.py:105-316`` ``PtTempoBackend``
 * ``oqupy/process_tensor.py:326-406``  ``get_mpo_tensor`` / ``compute_caps``
 * ``oqupy/system_dynamics.py:41-182, 631-700``  ``compute_dynamics``
@@ -311,6 +312,58 @@ def tempo_dynamics(initial_state, influence, unitary_transform, propagators,
     for _ in range(num_steps):
         out.append(o.compute_step()[1])
     return np.array(out), o
+
+
+class MeanFieldOracle:
+    """Restatement of ``MeanFieldTempoBackend`` (tempo_backend.py:629-773):
+    one ``TempoOracle`` per system, a coherent field advanced on the host.
+
+    ``propagators_list[i](step, field, field_derivative) -> (P1, P2)``;
+    ``compute_field(step, states, field, next_states) -> next field``;
+    ``compute_field_derivative(step, states, field) -> derivative``.
+    ``initialize() -> (0, states, field)``; ``compute_step() -> (step,
+    states, field)``.
+    """
+
+    def __init__(self, initial_state_list, initial_field, influence_list,
+                 unitary_transform_list, propagators_list, compute_field,
+                 compute_field_derivative, dkmax, epsrel):
+        self._field = complex(initial_field)
+        self._states = [np.array(s, dtype=CDT).reshape(-1) for s in initial_state_list]
+        self._propagators = list(propagators_list)
+        self._compute_field = compute_field
+        self._compute_field_derivative = compute_field_derivative
+        self._systems = []
+        for s, infl, u in zip(self._states, influence_list, unitary_transform_list):
+            ones = np.ones(s.size)
+            self._systems.append(TempoOracle(s, infl, u, None, ones, ones, dkmax, epsrel))
+        self._step = None
+
+    @property
+    def step(self):
+        return self._step
+
+    def initialize(self):
+        """tempo_backend.py:740-745."""
+        self._step = 0
+        for o in self._systems:
+            o.initialize()
+        return 0, [s.copy() for s in self._states], self._field
+
+    def compute_step(self):
+        """tempo_backend.py:747-773: the field derivative and the propagators
+        from the current states and field, one TEMPO step per system, then
+        the next field from the current and next states."""
+        cur = self._step
+        states = [s.copy() for s in self._states]
+        deriv = self._compute_field_derivative(cur, states, self._field)
+        props = [p(cur, self._field, deriv) for p in self._propagators]
+        nxt = [o.compute_system_step(cur + 1, np.asarray(p1, CDT), np.asarray(p2, CDT))
+               for o, (p1, p2) in zip(self._systems, props)]
+        self._field = complex(self._compute_field(cur, states, self._field, nxt))
+        self._states = nxt
+        self._step = cur + 1
+        return self._step, [s.copy() for s in nxt], self._field
 
 
 # ---------------------------------------------------------------------------
