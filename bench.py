@@ -762,6 +762,7 @@ def run_tempo(args, rank, world):
     d2h = 0
     states[:, 0] = np.array([np.asarray(x["rho0"]).reshape(-1) for x in local])
     done = 0
+    timelines = []   # (step, per-instance device-clock span of that step's launch)
     for k in range(args.steps):
         n = min(CHUNK, total_steps - done)
         if n <= 0:
@@ -783,6 +784,7 @@ def run_tempo(args, rank, world):
         if tuner is not None:
             tuner.end_chunk([e0.elapsed_time(e1) for e0, e1 in ev[done: done + n]])
         done += n
+        timelines.append((done, b.timeline()))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     clk = clocks.stop()
@@ -828,18 +830,22 @@ def run_tempo(args, rank, world):
                     "frac_le_1e-6": float(np.mean(td <= 1e-6))},
                 "complex128_sweeps64_per_split": sum(x["sweeps64"] for x in ic) / max(1, sum(x["splits"] for x in ic))}
 
-    # the last launch's timeline (device clock per instance): is a late step
+    # each chunk's last launch on the device clock, per instance: is a step
     # bound by its longest instance or by the sum of all instances' work?
-    tb = np.array([x["t_begin_ns"] for x in infos], dtype=np.int64)
-    te = np.array([x["t_end_ns"] for x in infos], dtype=np.int64)
-    dur = (te - tb) / 1e6
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    timeline = {"step": done, "launch_ms": float((te.max() - tb.min()) / 1e6),
-                "longest_instance_ms": float(dur.max()),
-                "instance_ms_sum_over_sms": float(dur.sum() / sms),
-                "instance_ms_p50": float(np.median(dur)), "sms": int(sms),
-                "note": ("per-instance device-clock span in the last launch: launch_ms close to "
-                         "longest_instance_ms means the step waits on one instance's split chain")}
+    timeline = {"sms": int(sms),
+                "note": ("per chunk, the device-clock spans of its last launch: launch_ms close to "
+                         "longest_instance_ms means the step waits on one instance's split chain; "
+                         "close to instance_ms_sum_over_sms, on the whole batch's work"),
+                "steps": []}
+    for step_no, tl in timelines:
+        dur = (tl[:, 1] - tl[:, 0]) / 1e6
+        timeline["steps"].append({
+            "step": step_no, "launch_ms": round(float((tl[:, 1].max() - tl[:, 0].min()) / 1e6), 3),
+            "longest_instance_ms": round(float(dur.max()), 3),
+            "longest_instance": int(np.argmax(dur)),
+            "instance_ms_sum_over_sms": round(float(dur.sum() / sms), 3),
+            "instance_ms_p50": round(float(np.median(dur)), 3)})
     nsplit = max(1, sum(x["splits"] for x in infos))
     stats = {"max_bond": max(x["max_bond"] for x in infos), "splits": nsplit,
              "sweeps64_per_split": sum(x["sweeps64"] for x in infos) / nsplit,
@@ -879,7 +885,7 @@ def run_tempo(args, rank, world):
                     "note": ("same run, wall clock: handle creation from host arrays (all inputs "
                              "host->device), every launch, every bench step's states device->host")},
             "clocks": clk, "gpu_launches": int(done), "mixed_stats": stats,
-            "last_launch_timeline": timeline,
+            "launch_timeline": timeline,
             "setup_seconds": setup_s,
             "ms_per_step_by_block": [float(ms[i:i + 50].sum()) / len(ms[i:i + 50]) for i in range(0, done, 50)],
             "accuracy_vs_fp64_oracle": acc}

@@ -222,6 +222,22 @@ otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t n_systems,
                        const double* rho0, int32_t num_steps, double* out,
                        void* stream);
 
+/* The same sweep with propagators that change from step to step and from
+ * system to system: compute_dynamics (system_dynamics.py:41-182) for
+ * time-dependent systems and with control operations, and the runs that
+ * compute_correlations_nt (system_dynamics.py:791-990) makes, one system
+ * slot per run.  props holds n_props pairs (P1 then P2, each D * D complex,
+ * transforms folded in as for otb_dyn_run); prop_index (n_systems *
+ * num_steps, host) names the pair system h uses at step k; a control
+ * operation is folded into the pairs on the host (a post-measurement
+ * control C of step k: P1 <- P1 C at step k; a pre-measurement control of
+ * step k + 1: P2 <- C P2 at step k; one of step 0: applied to rho0).
+ * Indices outside [0, n_props) are rejected before any device work. */
+otb_status otb_dyn_run_steps(otb_pt* h, int32_t inst, int32_t n_systems,
+                             const double* props, int32_t n_props,
+                             const int32_t* prop_index, const double* rho0,
+                             int32_t num_steps, double* out, void* stream);
+
 /* ----------------------------------------------- allocation-free TEMPO */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -259,30 +259,42 @@ extern "C" otb_status otb_pt_get_cap(otb_pt* h, int32_t inst, int32_t step, doub
   return OTB_OK;
 }
 
-extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const double* p1, const double* p2,
-                                  const double* rho0, int32_t num_steps, double* out, void* stream) {
+// The sweep of nh systems over process tensor inst: ptab holds n_props
+// propagator pairs (P1 then P2, D * D complex each), pidx (nh * num_steps,
+// host) the pair of system h at step k.  Every index is checked here, on the
+// host, before anything reaches the device.
+static otb_status dyn_run_impl(otb_pt* h, int32_t inst, int32_t nh, const double* ptab, int32_t n_props,
+                               const int32_t* pidx, const double* rho0, int32_t num_steps, double* out,
+                               void* stream) {
   otb_status st = pt_check(h, inst);
   if (st) return st;
   const PtDev& I = h->inst[inst];
-  if (!p1 || !p2 || !rho0 || !out || nh < 1 || nh > 1024 || num_steps < 0 || num_steps > I.num_steps)
+  if (!ptab || !rho0 || !out || nh < 1 || nh > 1024 || num_steps < 0 || num_steps > I.num_steps ||
+      n_props < 1 || (num_steps > 0 && !pidx))
     return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  for (long long e = 0; e < (long long)nh * num_steps; ++e)
+    if (pidx[e] < 0 || pidx[e] >= n_props)
+      return set_error(OTB_ERR_INVALID_ARG, "propagator index out of range");
   if ((st = pt_refresh(h, inst))) return st;
   if (!h->state[inst].caps_done) return set_error(OTB_ERR_INVALID_ARG, "process tensor not complete");
   std::vector<int2> dims;
   if ((st = pt_dims(h, inst, dims))) return st;
   const int D = I.D;
-  DevBuf dp1, dp2, drho, dv0, dv1, dout;
-  const size_t pb = (size_t)nh * D * D * 16, vb = (size_t)nh * I.cap * D * 16;
+  DevBuf dtab, didx, drho, dv0, dv1, dout;
+  const size_t tb = (size_t)n_props * 2 * D * D * 16, vb = (size_t)nh * I.cap * D * 16;
+  const size_t ib = (size_t)nh * std::max(num_steps, 1) * sizeof(int32_t);
   const size_t ob = (size_t)(num_steps + 1) * nh * D * 16;
   const int max_chunks = (I.cap + 31) / 32;
   DevBuf dpart, dcnt;
-  if (!dp1.alloc(pb) || !dp2.alloc(pb) || !drho.alloc((size_t)nh * D * 16) || !dv0.alloc(vb) ||
+  if (!dtab.alloc(tb) || !didx.alloc(ib) || !drho.alloc((size_t)nh * D * 16) || !dv0.alloc(vb) ||
       !dv1.alloc(vb) || !dout.alloc(ob) || !dpart.alloc((size_t)nh * max_chunks * D * 16) ||
       !dcnt.alloc((size_t)nh * sizeof(unsigned int)))
     return OTB_ERR_OOM;
   cudaStream_t s = (cudaStream_t)stream;
-  if (!check_cuda(cudaMemcpyAsync(dp1.p, p1, pb, cudaMemcpyHostToDevice, s), "upload") ||
-      !check_cuda(cudaMemcpyAsync(dp2.p, p2, pb, cudaMemcpyHostToDevice, s), "upload") ||
+  if (!check_cuda(cudaMemcpyAsync(dtab.p, ptab, tb, cudaMemcpyHostToDevice, s), "upload") ||
+      (num_steps > 0 &&
+       !check_cuda(cudaMemcpyAsync(didx.p, pidx, (size_t)nh * num_steps * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, s), "upload")) ||
       !check_cuda(cudaMemcpyAsync(drho.p, rho0, (size_t)nh * D * 16, cudaMemcpyHostToDevice, s), "upload") ||
       !check_cuda(cudaMemsetAsync(dout.p, 0, ob, s), "memset") ||
       !check_cuda(cudaMemsetAsync(dv0.p, 0, vb, s), "memset") ||
@@ -297,8 +309,9 @@ extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const dou
   L.dims = (const int2*)h->d_dims.p + I.dims_base;
   L.caps = (const double*)h->d_caps.p + 2 * I.caps_base;
   L.cap = I.cap;
-  L.p1 = (const double*)dp1.p;
-  L.p2 = (const double*)dp2.p;
+  L.ptab = (const double*)dtab.p;
+  L.pidx = (const int*)didx.p;
+  L.pidx_stride = num_steps;
   L.vcur = (double*)dv0.p;
   L.vnext = (double*)dv1.p;
   L.out = (double*)dout.p;
@@ -339,4 +352,29 @@ extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const dou
   cudaEventDestroy(ready);
   cudaStreamDestroy(cs);
   return ok ? OTB_OK : OTB_ERR_CUDA;
+}
+
+extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const double* p1, const double* p2,
+                                  const double* rho0, int32_t num_steps, double* out, void* stream) {
+  otb_status st = pt_check(h, inst);
+  if (st) return st;
+  if (!p1 || !p2 || nh < 1 || nh > 1024 || num_steps < 0)
+    return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  const int D = h->inst[inst].D;
+  const size_t dd = (size_t)2 * D * D;   // doubles of one D x D complex matrix
+  std::vector<double> tab((size_t)nh * 2 * dd);
+  for (int i = 0; i < nh; ++i) {
+    std::copy(p1 + i * dd, p1 + (i + 1) * dd, tab.begin() + (size_t)i * 2 * dd);
+    std::copy(p2 + i * dd, p2 + (i + 1) * dd, tab.begin() + (size_t)i * 2 * dd + dd);
+  }
+  std::vector<int32_t> idx((size_t)nh * std::max(num_steps, 1));
+  for (int i = 0; i < nh; ++i)
+    for (int k = 0; k < num_steps; ++k) idx[(size_t)i * num_steps + k] = i;
+  return dyn_run_impl(h, inst, nh, tab.data(), nh, idx.data(), rho0, num_steps, out, stream);
+}
+
+extern "C" otb_status otb_dyn_run_steps(otb_pt* h, int32_t inst, int32_t nh, const double* props,
+                                        int32_t n_props, const int32_t* prop_index, const double* rho0,
+                                        int32_t num_steps, double* out, void* stream) {
+  return dyn_run_impl(h, inst, nh, props, n_props, prop_index, rho0, num_steps, out, stream);
 }

@@ -5,11 +5,16 @@
 // _apply_caps (:643-651).  For a rank-3 PT-MPO tensor T_k[l][r][a] (delta
 // between input and output legs, process_tensor.py:346-347) one step of
 // system h is
-//     u[l][a]  = sum_b P1_h[a][b] v[l][b]
+//     u[l][a]  = sum_b P1_hk[a][b] v[l][b]
 //     w[r][a]  = sum_l u[l][a] T_k[l][r][a]          (T_k = d * site_k[l][a][r])
-//     v'[r][a] = sum_b P2_h[a][b] w[r][b]
+//     v'[r][a] = sum_b P2_hk[a][b] w[r][b]
 //     rho_h(k+1)[a] = sum_r v'[r][a] cap_{k+1}[r]
-// One launch per step (grid: bond chunks x systems); the host replays the
+// (P1_hk, P2_hk) is entry pidx[h][k] of a table of propagator pairs: a
+// time-dependent system has one pair per step, and control operations
+// (system_dynamics.py:131-160) are folded into the pairs of their steps on
+// the host -- a post-measurement control of step k into P1_hk (P1 post_k),
+// a pre-measurement control of step k+1 into P2_hk (pre_{k+1} P2).  One
+// launch per step (grid: bond chunks x systems); the host replays the
 // launches of a whole sweep as a CUDA graph.  A transform_in / transform_out
 // of the process tensor is folded into P1 / P2 on the host.  The read-out
 // sum is reproducible bit for bit: a CTA adds its bond chunk's terms in a
@@ -37,8 +42,8 @@ __global__ void __launch_bounds__(DYN_THREADS) dyn_step_kernel(DynLaunch L) {
   zc* u = (zc*)dsm;
   zc* w = u + l * D;
   const zc* v = (const zc*)L.vcur + (long long)h * L.cap * D;
-  const zc* P1 = (const zc*)L.p1 + (long long)h * D * D;
-  const zc* P2 = (const zc*)L.p2 + (long long)h * D * D;
+  const zc* P1 = (const zc*)L.ptab + (long long)L.pidx[(long long)h * L.pidx_stride + k] * 2 * D * D;
+  const zc* P2 = P1 + D * D;
   for (int idx = tid; idx < l * D; idx += nt) {
     const int ll = idx / D, a = idx - ll * D;
     zc acc = mk<double>(0, 0);

@@ -136,8 +136,9 @@ struct DynLaunch {
   const int2* dims;     // per step (l, r)
   const double* caps;   // (num_steps + 1) * cap
   int cap;
-  const double* p1;     // nh * D * D (eigenbasis-folded)
-  const double* p2;
+  const double* ptab;   // propagator pairs (P1 then P2, D * D complex each)
+  const int* pidx;      // nh * pidx_stride: pair of system h at step k
+  int pidx_stride;
   double* vcur;         // nh * cap * D
   double* vnext;
   double* out;          // (num_steps + 1) * nh * D

@@ -19,12 +19,15 @@ GPU build, a ``DeviceProcessTensor`` (``device_pt.py``): a
 
 ``compute_dynamics`` has no configuration argument
 (oqupy/system_dynamics.py:41-53): the wrapper routes a call to the GPU sweep
-when its single process tensor is a ``DeviceProcessTensor``, there is no
-control and ``record_all`` is set, and otherwise calls the reference
-function (a ``DeviceProcessTensor`` that the reference must handle is
+when its single process tensor is a ``DeviceProcessTensor``, the system is a
+``System`` or ``TimeDependentSystem`` and ``record_all`` is set (control
+operations are folded into the sweep's propagators, ``correlations.py``),
+and otherwise calls the reference function (a ``DeviceProcessTensor`` that the reference must handle is
 first copied to a host ``SimpleProcessTensor``).  Both
 ``oqupy.system_dynamics.compute_dynamics`` and ``oqupy.compute_dynamics``
-(bound at import, oqupy/__init__.py:104) are rebound.
+(bound at import, oqupy/__init__.py:104) are rebound, and so is
+``compute_correlations_nt`` (which ``compute_correlations`` calls): on a
+device process tensor its runs become the slots of one batched sweep.
 """
 
 from typing import Any, Dict, Optional
@@ -126,6 +129,8 @@ def install(oqupy_module: Any = None) -> None:
         def host_copy(pt):
             return pt.to_host(ptm.SimpleProcessTensor) if isinstance(pt, dev_cls) else pt
 
+        gpu_systems = (sys_mod.System, sys_mod.TimeDependentSystem)
+
         def compute_dynamics(system, initial_state=None, dt=None, num_steps=None,
                              start_time=0.0, process_tensor=None, control=None,
                              record_all=True, subdiv_limit=None,
@@ -140,8 +145,8 @@ def install(oqupy_module: Any = None) -> None:
                 kwargs["liouvillian_epsrel"] = liouvillian_epsrel
             pts = process_tensor if isinstance(process_tensor, list) else \
                 ([] if process_tensor is None else [process_tensor])
-            gpu = (len(pts) == 1 and isinstance(pts[0], dev_cls) and control is None
-                   and record_all and type(system) is sys_mod.System)
+            gpu = (len(pts) == 1 and isinstance(pts[0], dev_cls) and record_all
+                   and type(system) in gpu_systems)
             if not gpu:
                 if any(isinstance(p, dev_cls) for p in pts):
                     hosts = [host_copy(p) for p in pts]
@@ -155,10 +160,26 @@ def install(oqupy_module: Any = None) -> None:
             args = [dt, start_time]
             args.append(kwargs.get("subdiv_limit", sd_mod.SUBDIV_LIMIT))
             args.append(kwargs.get("liouvillian_epsrel", sd_mod.INTEGRATE_EPSREL))
-            p1, p2 = system.get_propagators(*args)(0)
-            from .pt import device_compute_dynamics
-            st = device_compute_dynamics(pts[0], [(p1, p2)],
-                                         [initial_state.reshape(-1)], num_steps)
+            props = system.get_propagators(*args)
+            if type(system) is sys_mod.System:
+                p1, p2 = props(0)
+
+                def props(step, pair=(p1, p2)):
+                    return pair
+            ctl = None
+            if control is not None:
+                # Control.get_controls per step (control.py:119-180), as the
+                # reference's loop asks for them (system_dynamics.py:109-114)
+                ctl = {"pre": {}, "post": {}}
+                for step in range(num_steps + 1):
+                    pre, post = control.get_controls(step, dt=dt, start_time=start_time)
+                    if pre is not None:
+                        ctl["pre"][step] = pre
+                    if post is not None:
+                        ctl["post"][step] = post
+            from . import correlations as corr
+            st = corr.device_dynamics(pts[0], [props], [initial_state.reshape(-1)],
+                                      num_steps, [ctl])
             states = [s.reshape(hs_dim, hs_dim) for s in st[:, 0]]
             times = start_time + np.arange(len(states)) * dt
             return dyn_mod.Dynamics(times=list(times), states=states)
@@ -167,6 +188,58 @@ def install(oqupy_module: Any = None) -> None:
         sd_mod.compute_dynamics = compute_dynamics
         if _installed["compute_dynamics_pkg"] is not None:
             oqupy_module.compute_dynamics = compute_dynamics
+
+        # compute_correlations_nt (system_dynamics.py:791-990; also reached
+        # through compute_correlations, :1011-1093): on a device process
+        # tensor, every compute_dynamics run of its schedule becomes one slot
+        # of a single batched sweep
+        ref_nt = sd_mod.compute_correlations_nt
+        _installed["compute_correlations_nt"] = ref_nt
+        _installed["compute_correlations_nt_pkg"] = getattr(oqupy_module, "compute_correlations_nt", None)
+
+        def compute_correlations_nt(system, process_tensor, operators, ops_times, ops_order,
+                                    initial_state=None, start_time=0.0, dt=None,
+                                    progress_type=None):
+            if not (isinstance(process_tensor, dev_cls) and type(system) in gpu_systems
+                    and initial_state is not None):
+                if isinstance(process_tensor, dev_cls):
+                    process_tensor = host_copy(process_tensor)
+                return ref_nt(system, process_tensor, operators, ops_times, ops_order,
+                              initial_state=initial_state, start_time=start_time, dt=dt,
+                              progress_type=progress_type)
+            # the reference's input checks and time parsing (:847-901)
+            dim = system.dimension
+            assert process_tensor.hilbert_space_dimension == dim
+            for op in operators:
+                assert np.asarray(op).shape == (dim, dim)
+            assert isinstance(start_time, float)
+            if dt is None:
+                assert process_tensor.dt is not None, \
+                    "It is necessary to specify time step `dt` because the given tensor has none."
+                dt_ = process_tensor.dt
+            else:
+                dt_ = dt
+            assert len(operators) == len(ops_times) == len(ops_order), \
+                "Lengths of the lists ops_order, ops_times and dip_ops do not match."
+            max_step = len(process_tensor)
+            steps = [sd_mod._parse_times(t, max_step, dt_, start_time) for t in ops_times]
+            ret_times = [start_time + dt_ * s for s in steps]
+            props = system.get_propagators(dt_, start_time, sd_mod.SUBDIV_LIMIT,
+                                           sd_mod.INTEGRATE_EPSREL)
+            if type(system) is sys_mod.System:
+                p1, p2 = props(0)
+
+                def props(step, pair=(p1, p2)):
+                    return pair
+            from . import correlations as corr
+            rho0 = np.asarray(initial_state, dtype=np.complex128).reshape(-1)
+            return ret_times, corr.device_correlations_nt(process_tensor, props, rho0,
+                                                          operators, steps, ops_order)
+
+        compute_correlations_nt.reference_function = ref_nt
+        sd_mod.compute_correlations_nt = compute_correlations_nt
+        if _installed["compute_correlations_nt_pkg"] is not None:
+            oqupy_module.compute_correlations_nt = compute_correlations_nt
 
 
 def uninstall(oqupy_module: Any = None) -> None:
@@ -189,3 +262,7 @@ def uninstall(oqupy_module: Any = None) -> None:
         pkg = _installed.pop("compute_dynamics_pkg", None)
         if pkg is not None:
             oqupy_module.compute_dynamics = pkg
+        sd_mod.compute_correlations_nt = _installed.pop("compute_correlations_nt")
+        pkg = _installed.pop("compute_correlations_nt_pkg", None)
+        if pkg is not None:
+            oqupy_module.compute_correlations_nt = pkg

@@ -148,6 +148,29 @@ class PtBatch:
                                         ctypes.c_void_p(stream or 0)))
         return out.view(np.complex128)[..., 0]
 
+    def dynamics_steps(self, i: int, props, prop_index, rho0, num_steps: int,
+                       stream: Optional[int] = None) -> np.ndarray:
+        """compute_dynamics for ``H`` systems whose propagators change per
+        step (``otb_dyn_run_steps``).  ``props``: ``[n_props, 2, D, D]``
+        pairs (transforms and control operations already folded in);
+        ``prop_index``: ``[H, num_steps]`` pair of system h at step k;
+        ``rho0``: ``[H, D]``.  Returns states ``[num_steps+1, H, D]``."""
+        D = self.meta[i]["D"]
+        tab = nat.cplx(np.asarray(props, dtype=np.complex128).reshape(-1, 2, D, D))
+        n = int(num_steps)
+        r0a = np.asarray(rho0, dtype=np.complex128).reshape(-1, D)
+        H = r0a.shape[0]
+        idx = np.zeros((H, max(n, 1)), dtype=np.int32)
+        if n:
+            idx[:] = np.asarray(prop_index, dtype=np.int32).reshape(H, n)
+        r0 = nat.cplx(r0a)
+        out = np.zeros((n + 1, H, D, 2))
+        nat.check(nat.lib().otb_dyn_run_steps(
+            self._h, int(i), H, nat.dptr(tab), int(tab.shape[0]),
+            idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nat.dptr(r0), n,
+            nat.dptr(out), ctypes.c_void_p(stream or 0)))
+        return out.view(np.complex128)[..., 0]
+
 
 class GpuPtTempoBackend:
     """Drop-in for ``oqupy.backends.pt_tempo_backend.PtTempoBackend``

@@ -507,9 +507,13 @@ def pt_mpo_rank4(T3: np.ndarray, transform_in=None, transform_out=None):
 
 
 def compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps,
-                        num_steps=None, transform_in=None, transform_out=None):
-    """``compute_dynamics`` with one process tensor and no controls
-    (system_dynamics.py:41-182, helpers :631-700).  Returns
+                        num_steps=None, transform_in=None, transform_out=None,
+                        controls=None):
+    """``compute_dynamics`` with one process tensor (system_dynamics.py:41-182,
+    helpers :631-700).  ``controls(step) -> (pre, post)`` superoperators or
+    ``None`` (``Control.get_controls``, control.py:119-160): ``pre`` acts
+    before the state of the step is read, ``post`` after it, before the
+    step's propagation (system_dynamics.py:131-160).  Returns
     ``states[num_steps+1, D]``."""
     rho = np.asarray(initial_state, dtype=CDT).reshape(-1)
     D = rho.size
@@ -517,8 +521,15 @@ def compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps,
         num_steps = len(mpo_tensors)
     v = rho.reshape(1, D)
     states = []
-    for step in range(num_steps):
+    for step in range(num_steps + 1):
+        pre, post = controls(step) if controls is not None else (None, None)
+        if pre is not None:
+            v = v @ np.asarray(pre, CDT).T
+        if step == num_steps:
+            break
         states.append(np.einsum("ba,b->a", v, caps[step]))
+        if post is not None:
+            v = v @ np.asarray(post, CDT).T
         p1, p2 = propagators(step)
         v = v @ np.asarray(p1, CDT).T
         T = pt_mpo_rank4(mpo_tensors[step], transform_in, transform_out)
@@ -526,6 +537,45 @@ def compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps,
         v = v @ np.asarray(p2, CDT).T
     states.append(np.einsum("ba,b->a", v, caps[num_steps]))
     return np.array(states)
+
+
+def correlations_nt_pt(initial_state, propagators, mpo_tensors, caps, operators,
+                       op_steps, ops_order, transform_in=None, transform_out=None):
+    """``compute_correlations_nt`` (system_dynamics.py:791-990) for operator
+    time steps already parsed to integers: for every combination of the
+    first n-1 operators' steps (time-ordered, else skipped), one
+    ``compute_dynamics`` run with each of those operators as a
+    pre-measurement control at its step (``left``: A rho, ``right``: rho A;
+    operators.py:139-147), read out as the expectation of the last operator
+    at every last-operator step not before the latest first step.  Returns
+    the array ``[len(op_steps[0]), ..., len(op_steps[-1])]`` with NaN where
+    the reference leaves NaN."""
+    from itertools import product
+    d = int(round(np.sqrt(np.asarray(initial_state).size)))
+    eye = np.identity(d)
+    sups = [np.kron(op, eye) if o == "left" else np.kron(eye, np.asarray(op).T)
+            for op, o in zip(operators, ops_order)]
+    out = np.full([len(t) for t in op_steps], np.nan + 1j * np.nan, dtype=CDT)
+    last = np.asarray(op_steps[-1])
+    for idx in product(*[range(len(t)) for t in op_steps[:-1]]):
+        first = [int(op_steps[j][i]) for j, i in enumerate(idx)]
+        if first != sorted(first):
+            continue
+        keep = np.flatnonzero(last >= max(first))
+        if keep.size == 0:
+            continue
+        ctrl = {}
+        for j, st in enumerate(first):
+            ctrl[st] = sups[j] if st not in ctrl else sups[j] @ ctrl[st]
+        nsteps = int(last[keep].max())
+        states = compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps, nsteps,
+                                     transform_in, transform_out,
+                                     controls=lambda s: (ctrl.get(s), None))
+        op = np.asarray(operators[-1])
+        for k in keep:
+            rho = states[int(last[k])].reshape(d, d)
+            out[idx + (k,)] = np.trace(op @ rho)
+    return out
 
 
 # ---------------------------------------------------------------------------

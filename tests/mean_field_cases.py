@@ -155,33 +155,8 @@ def backend_args(name, fixture):
         dkmax=None if dkmax < 0 else dkmax, epsrel=case["epsrel"])
 
 
+
 def patch_field_hamiltonian_check(oqupy):
-    """The reference checks a field-dependent Hamiltonian and time-dependent
-    Lindblad operators by wrapping them in ``np.vectorize``
-    (oqupy/system.py:996-1005, 1045-1074) and keeps the wrappers; numpy 2.5
-    no longer converts the matrix such a wrapper returns for scalar
-    arguments.  Replace the matrix-valued wrappers by the callables
-    themselves, with the same checks; a scalar call returns the same matrix
-    either way.  (Idempotent.)"""
-    sysm = oqupy.system
-    if getattr(sysm, "_vectorize_patched", False):
-        return
-
-    def check_h(hamiltonian):
-        h = np.asarray(hamiltonian(1.0, 1.0 + 1.0j))
-        if h.ndim != 2 or h.shape[0] != h.shape[1]:
-            raise AssertionError("Time and field dependent Hamiltonian must return a square matrix.")
-        return hamiltonian
-
-    ref_lists = sysm._check_dissipator_lists
-
-    def check_gl(gammas, lindblad_operators):
-        gammas, lindblad_operators = ref_lists(gammas, lindblad_operators)
-        for g in gammas:
-            float(g(1.0))
-        for op in lindblad_operators:
-            np.array(op(1.0))
-        return [np.vectorize(g) for g in gammas], list(lindblad_operators)
-    sysm._check_tfielddependent_hamiltonian = check_h
-    sysm._check_tdependent_gammas_lindblad_operators = check_gl
-    sysm._vectorize_patched = True
+    """See ``tests/reference_compat.py``."""
+    from tests.reference_compat import patch_vectorize_checks
+    patch_vectorize_checks(oqupy)

@@ -74,7 +74,6 @@ def test_device_process_tensor_matches_simple_process_tensor():
 def test_compute_dynamics_routes_device_process_tensors(monkeypatch):
     oqupy = import_reference()
     import oqupy_gb300
-    from oqupy_gb300 import pt as ptmod
     from oqupy_gb300.device_pt import device_process_tensor_class
     g, mpos, caps = _build()
     pt = oqupy.SimpleProcessTensor(g["d"], g["dt"])
@@ -83,14 +82,15 @@ def test_compute_dynamics_routes_device_process_tensors(monkeypatch):
     pt.compute_caps()
     calls = []
 
-    def fake(process_tensor, pairs, rho0s, num_steps=None):
-        calls.append(len(pairs))
-        p1, p2 = pairs[0]
-        st = to.compute_dynamics_pt(rho0s[0], lambda s: (p1, p2), mpos, caps,
+    def fake(process_tensor, propagators, rho0s, num_steps, controls=None):
+        calls.append(len(propagators))
+        assert controls == [None]
+        st = to.compute_dynamics_pt(rho0s[0], propagators[0], mpos, caps,
                                     num_steps=num_steps)
         return st[:, None, :]
 
-    monkeypatch.setattr(ptmod, "device_compute_dynamics", fake)
+    from oqupy_gb300 import correlations
+    monkeypatch.setattr(correlations, "device_dynamics", fake)
     system = oqupy.System(np.array([[0.3, 0.5], [0.5, -0.3]]))
     rho0 = np.array([[1.0, 0], [0, 0]], dtype=complex)
     oqupy_gb300.install(oqupy)
