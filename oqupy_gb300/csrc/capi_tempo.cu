@@ -256,8 +256,9 @@ extern "C" otb_status otb_tempo_create(const otb_tempo_config* cfg, int32_t n,
                                cudaMemcpyHostToDevice),
                     "init dims"))
       return OTB_ERR_CUDA;
-    if (!check_cuda(cudaMemcpy((double*)h->d_out.p + 2 * I.out_base, r0.data(),
-                               r0.size() * sizeof(double), cudaMemcpyHostToDevice),
+    // the output ring holds complex128 states in both forms
+    if (!check_cuda(cudaMemcpy((double*)h->d_out.p + 2 * I.out_base, ins[i].rho0,
+                               2 * D * sizeof(double), cudaMemcpyHostToDevice),
                     "init out"))
       return OTB_ERR_CUDA;
   }

@@ -20,8 +20,14 @@ oracle's spread under 1e-15 / 1e-14 / 1e-9 relative input perturbations
   MPS bond profile identical to the oracle's after every step;
 * from the first ill-conditioned step on: within 10x the oracle's largest
   spread over the run (complex128: the 1e-15 / 1e-14 / gesvd spreads;
-  mixed: those and the 1e-9 spread, the scale of its QR cut), and never
-  above 1e-6 (mixed: max(1e-6, ...)).
+  mixed: those and the 1e-9 spread, the scale of its QR cut; mixed: never
+  below 1e-6).  Where the step was flagged by a cut gap below ``GAP_TOL``,
+  the bar is at least the instance's epsrel: which member of a pair equal
+  to that precision is kept is decided by rounding, swapping them changes
+  the split by the dropped member's weight -- at most the truncation
+  threshold, epsrel relative -- and at gaps far below rounding x condition
+  (a 6e-12 gap occurs among the qutrit draws) the response to one more
+  rounding-level perturbation is not bounded by the sampled ones.
 
 Each case prints, per draw, the worst error, the first step above 1e-10, the
 first ill-conditioned step, the first bond-profile divergence and the
@@ -115,6 +121,8 @@ def check_draws(kind, precision):
         clean_tol = gc.PARITY_ABS if precision == "complex128" else gc.MIXED_ABS
         after_tol = max(clean_tol, gc.ENVELOPE_FACTOR * spread)
         tol = np.where(np.arange(n + 1) < ill, clean_tol, after_tol)
+        gap_ill = next((s for s in range(1, n + 1) if g["gap"][i][s - 1] < GAP_TOL), n + 1)
+        tol[gap_ill:] = np.maximum(tol[gap_ill:], float(g["epsrel"][i]))
         bad = np.flatnonzero(err > tol)
         ref_bonds = g["bonds"][i]
         bdiv = next((s + 1 for s in range(n)
