@@ -694,7 +694,7 @@ def tempo_workload_config(n, timed_steps):
                          "wc U[1,10], T U[0,5], Omega U[0.5,2], dkmax U{20..300}, dt 0.05, "
                          "epsrel 1e-6), whole 500-step trajectories"),
             "instances": n, "seed": BATCH_SEED,
-            "bench_step": f"{CHUNK} TEMPO time steps of every instance ({CHUNK} launches)",
+            "bench_step": f"{CHUNK} TEMPO time steps of every instance",
             "timed_steps": f"1..{timed_steps} of {NSTEPS_TRAJ}",
             "l2": "GPU arm: flushed (256 MiB write) before every bench step; site rings >> L2"}
 
@@ -747,7 +747,7 @@ def run_tempo(args, rank, world):
         torch.cuda.synchronize()
 
     from oqupy_gb300.autotune import BucketTuner
-    tuner = BucketTuner() if args.autotune else None
+    tuner = BucketTuner() if args.autotune and args.launch_steps <= 1 else None
     D = 4
     states = np.zeros((len(local), total_steps + 1, D), dtype=np.complex128)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -762,6 +762,8 @@ def run_tempo(args, rank, world):
     d2h = 0
     states[:, 0] = np.array([np.asarray(x["rho0"]).reshape(-1) for x in local])
     done = 0
+    ls = max(1, int(args.launch_steps))
+    launches = []    # (first step, steps) of every timed launch
     timelines = []   # (step, per-instance device-clock span of that step's launch)
     for k in range(args.steps):
         n = min(CHUNK, total_steps - done)
@@ -771,25 +773,33 @@ def run_tempo(args, rank, world):
         if tuner is not None:
             tuner.begin_chunk(b.max_bond() if done else 1)
         cur = None
-        for j in range(n):
+        j = 0
+        while j < n:
             if tuner is not None and tuner.shape_for(j) != cur:
                 cur = tuner.shape_for(j)
                 b.set_launch(cur[0], cur[1])
+            m = min(ls, n - j)
             ev[done + j][0].record(dev_stream)
-            b.advance(1, dev_stream.cuda_stream)
+            b.advance(m, dev_stream.cuda_stream)        # one launch, m steps of every instance
             ev[done + j][1].record(dev_stream)
+            launches.append((done + j, m))
+            j += m
         chunk_states = b.states(done + 1, n)             # device -> host (synchronises)
         states[:, done + 1: done + 1 + n] = chunk_states
         d2h += chunk_states.nbytes
         if tuner is not None:
-            tuner.end_chunk([e0.elapsed_time(e1) for e0, e1 in ev[done: done + n]])
+            tuner.end_chunk([ev[s0][0].elapsed_time(ev[s0][1]) / m
+                             for s0, m in launches if done <= s0 < done + n])
         done += n
         timelines.append((done, b.timeline()))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     clk = clocks.stop()
     b.check_status()
-    ms = np.array([e0.elapsed_time(e1) for e0, e1 in ev[:done]])
+    # per-step times: a launch of m steps contributes its time / m to each
+    ms = np.zeros(done)
+    for s0, m in launches:
+        ms[s0: s0 + m] = ev[s0][0].elapsed_time(ev[s0][1]) / m
     infos = [b.info(i) for i in range(b.n)]
     b.close()
     flops = float(sum(x["flops_alg"] for x in infos))
@@ -875,6 +885,7 @@ def run_tempo(args, rank, world):
             "data": "synthetic (seeded draws of the batched spin-boson distribution)",
             "config": tempo_workload_config(len(insts), done),
             "arm": {"precision": "mixed", "parallelism": f"instances x {world} GPUs",
+                    "steps_per_launch": ls,
                     "warmup": f"{args.warmup} bench steps on a separate batch (seed {BATCH_SEED + 7919})",
                     "launch": ({"autotuned_per_bond_bucket": tuner.table()} if tuner is not None
                                else {"block": args.block or 256, "smem_kb": args.smem_kb or 56})},
@@ -884,7 +895,7 @@ def run_tempo(args, rank, world):
                     "d2h_bytes_per_step": int(d2h // max(1, args.steps)),
                     "note": ("same run, wall clock: handle creation from host arrays (all inputs "
                              "host->device), every launch, every bench step's states device->host")},
-            "clocks": clk, "gpu_launches": int(done), "mixed_stats": stats,
+            "clocks": clk, "gpu_launches": len(launches), "mixed_stats": stats,
             "launch_timeline": timeline,
             "setup_seconds": setup_s,
             "ms_per_step_by_block": [float(ms[i:i + 50].sum()) / len(ms[i:i + 50]) for i in range(0, done, 50)],
@@ -944,6 +955,9 @@ def main():
                     help="first TEMPO steps timed in the complex128 form for the comparison")
     ap.add_argument("--chi-cap", type=int, default=64)
     ap.add_argument("--block", type=int, default=0, help="threads per CTA (0 = the library default)")
+    ap.add_argument("--launch-steps", type=int, default=1,
+                    help="TEMPO steps per launch (instances are independent: a launch of m steps "
+                         "lets every CTA run its instance m steps without a grid-wide wait)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="fixed launch shape instead of the per-bond-bucket tuner")
     ap.add_argument("--smem-kb", type=int, default=0, help="dynamic shared memory per CTA (0 = default)")

@@ -316,6 +316,9 @@ extern "C" otb_status otb_tempo_advance(otb_tempo* h, int32_t nsteps, void* stre
   }
   cudaStream_t s = (cudaStream_t)stream;
   if (!check_cuda(cudaMemsetAsync(h->d_queue.p, 0, sizeof(int), s), "reset queue")) return OTB_ERR_CUDA;
+  // longest instance of the previous launch first (a launch waits on it)
+  if (!check_cuda(launch_tempo_order((InstState*)h->d_state.p, (int*)h->d_order.p, h->n, s), "order"))
+    return OTB_ERR_CUDA;
   TempoLaunch L;
   L.n = h->n;
   L.inst = (const InstDev*)h->d_inst.p;

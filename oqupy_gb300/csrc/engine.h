@@ -67,6 +67,7 @@ inline long long tempo_work_bytes(long long wcap) { return wcap * (3 * 16 + 16);
 // precision: 0 = complex128 (FP64 Jacobi), 1 = mixed (double-float Jacobi
 // on the FP32 pipe; FP64 sites, contractions, rotation angles, norms, rank
 // decisions and read-out)
+cudaError_t launch_tempo_order(InstState* state, int* order, int n, cudaStream_t stream);
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,
                          int smem_bytes, cudaStream_t stream);
 int tempo_smem_bytes(int precision);

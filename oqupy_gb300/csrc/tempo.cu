@@ -30,6 +30,7 @@
 // with their operands converted once per element (ff.cuh: ccacc_fma).
 #include <math.h>
 
+#include <climits>
 #include <cmath>
 
 #include "../../include/oqupy_gb300.h"
@@ -612,6 +613,62 @@ int tempo_smem_bytes(int precision) {
   // the static SharedStep block)
   (void)precision;
   return 88 * 1024;
+}
+
+// Work-queue order for the next launch: instances by the device time they
+// took in the previous launch, longest first (ties and instances not yet
+// timed keep their current relative order).  A launch waits on its longest
+// instance, so that one should start first.  One CTA, bitonic sort of
+// (time, position) pairs in shared memory; n <= ORDER_MAX_N (larger batches
+// keep their static order).
+constexpr int ORDER_MAX_N = 2048;   // 32 KiB of static shared memory
+constexpr int ORDER_THREADS = 1024;
+
+__global__ void __launch_bounds__(ORDER_THREADS) tempo_order_kernel(const InstState* state, int* order, int n) {
+  __shared__ long long key[ORDER_MAX_N];
+  __shared__ int pos[ORDER_MAX_N];
+  __shared__ int cur[ORDER_MAX_N];
+  int n2 = 1;
+  while (n2 < n) n2 <<= 1;
+  for (int j = threadIdx.x; j < n2; j += blockDim.x) {
+    if (j < n) {
+      const int i = order[j];
+      cur[j] = i;
+      const InstState st = state[i];
+      key[j] = (st.t_end_ns > st.t_begin_ns) ? (st.t_end_ns - st.t_begin_ns) : -1;
+    } else {
+      key[j] = LLONG_MIN;
+    }
+    pos[j] = j;
+  }
+  __syncthreads();
+  // descending key, ascending position among equal keys
+  for (int size = 2; size <= n2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
+        const int lo = 2 * t - (t & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = ((lo & size) == 0);
+        const long long ka = key[lo], kb = key[hi];
+        const int pa = pos[lo], pb = pos[hi];
+        const bool a_first = (ka > kb) || (ka == kb && pa < pb);
+        if (a_first != up) {
+          key[lo] = kb;
+          key[hi] = ka;
+          pos[lo] = pb;
+          pos[hi] = pa;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) order[j] = cur[pos[j]];
+}
+
+cudaError_t launch_tempo_order(InstState* state, int* order, int n, cudaStream_t stream) {
+  if (n < 2 || n > ORDER_MAX_N) return cudaSuccess;
+  tempo_order_kernel<<<1, ORDER_THREADS, 0, stream>>>(state, order, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_tempo(const TempoLaunch& L, int precision, int grid, int block,

@@ -45,6 +45,7 @@ class GpuMeanFieldTempoBackend:
         for sn, sw in zip(sum_north_list, sum_west_list):
             if not (np.allclose(sn, 1.0) and np.allclose(sw, 1.0)):
                 raise NotImplementedError("the GPU TEMPO engine needs all-ones sums")
+        self._initial_state_list = initial_state_list   # as given (returned by initialize)
         self._initial_states = [np.array(s, dtype=np.complex128).reshape(-1)
                                 for s in initial_state_list]
         self._initial_field = complex(initial_field)
@@ -98,7 +99,9 @@ class GpuMeanFieldTempoBackend:
         self._history = []
         self._step = 0
         self._field = self._initial_field
-        self._states = [s.copy() for s in self._initial_states]
+        # the step-0 states are the initial states as given, as in the
+        # reference (tempo_backend.py:740-745); later ones are vectors
+        self._states = deepcopy(list(self._initial_state_list))
         return self._step, deepcopy(self._states), self._field
 
     def _new_batch(self):
