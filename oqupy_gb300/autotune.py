@@ -31,23 +31,26 @@ CANDIDATES: List[Tuple[int, int, int]] = [
 
 
 # (threads per CTA, dynamic smem KiB): narrow CTAs, three per SM / one wide CTA per SM
-BUCKET_CANDIDATES: List[Tuple[int, int]] = [(256, 56), (512, 200)]
+BUCKET_CANDIDATES: List[Tuple[int, int]] = [(512, 200), (256, 56)]
 
 
 class BucketTuner:
     """Launch shape per bond bucket (``bucket_width`` bond values each).
 
     ``shape_for(step_in_chunk)`` gives the shape of a launch in the current
-    chunk; ``end_chunk(times)`` takes the chunk's per-launch event times and
-    settles an untuned bucket (mean time per shape over its interleaved
-    launches); ``begin_chunk(max_bond)`` selects the bucket of the next
-    chunk.  Pure policy: the caller applies shapes (``TempoBatch.set_launch``)
-    and times launches."""
+    chunk: in the first chunk of an untuned bucket the first ``trials``
+    launches per candidate alternate the candidates and the rest of the chunk
+    uses the first candidate; ``end_chunk(times)`` takes the chunk's
+    per-launch event times and settles the bucket (mean time per shape over
+    the interleaved trial launches); ``begin_chunk(max_bond)`` selects the
+    bucket of the next chunk.  Pure policy: the caller applies shapes
+    (``TempoBatch.set_launch``) and times launches."""
 
     def __init__(self, candidates: Sequence[Tuple[int, int]] = BUCKET_CANDIDATES,
-                 bucket_width: int = 8):
+                 bucket_width: int = 8, trials: int = 2):
         self.candidates = list(candidates)
         self.width = int(bucket_width)
+        self.n_trial = max(1, int(trials)) * len(self.candidates)
         self.best: Dict[int, Tuple[int, int]] = {}
         self.trials: Dict[int, Dict[Tuple[int, int], float]] = {}
         self.bucket = 0
@@ -60,14 +63,14 @@ class BucketTuner:
 
     def shape_for(self, k: int) -> Tuple[int, int]:
         if self.tuning():
-            return self.candidates[k % len(self.candidates)]
+            return self.candidates[k % len(self.candidates)] if k < self.n_trial else self.candidates[0]
         return self.best[self.bucket]
 
     def end_chunk(self, times_ms: Sequence[float]):
         if not self.tuning() or not times_ms:
             return
         acc: Dict[Tuple[int, int], List[float]] = {}
-        for k, t in enumerate(times_ms):
+        for k, t in enumerate(list(times_ms)[: self.n_trial]):
             acc.setdefault(self.shape_for(k), []).append(float(t))
         means = {c: sum(v) / len(v) for c, v in acc.items()}
         self.trials[self.bucket] = means

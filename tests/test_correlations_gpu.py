@@ -24,7 +24,7 @@ def gpu_pt(g, name, precision):
     d = int(g[f"{name}/d"])
     b = PtBatch([dict(hs_dim=d, num_steps=int(g[f"{name}/nsteps"]), dkmax=int(g[f"{name}/dkmax"]),
                       epsrel=float(g[f"{name}/epsrel"]), influences=g[f"{name}/influences"])],
-                precision=precision, chi_cap=64)
+                precision=precision, chi_cap=min(128, 1152 // (d * d)))
     b.build()
 
     class Pt:

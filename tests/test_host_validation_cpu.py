@@ -52,9 +52,10 @@ def test_bucket_tuner_alternates_then_keeps_the_faster_shape():
     t = BucketTuner(candidates=[(256, 56), (512, 200)], bucket_width=8)
     t.begin_chunk(5)
     assert t.tuning()
-    shapes = [t.shape_for(k) for k in range(4)]
-    assert shapes == [(256, 56), (512, 200), (256, 56), (512, 200)]
-    t.end_chunk([10.0, 14.0, 11.0, 15.0])           # narrow CTAs faster
+    shapes = [t.shape_for(k) for k in range(6)]
+    # two trial launches per candidate, then the first candidate
+    assert shapes == [(256, 56), (512, 200), (256, 56), (512, 200), (256, 56), (256, 56)]
+    t.end_chunk([10.0, 14.0, 11.0, 15.0, 30.0, 30.0])   # narrow CTAs faster in the trials
     assert not t.tuning() and t.shape_for(0) == (256, 56)
     t.begin_chunk(30)                               # a new bucket is tuned again
     assert t.tuning()
