@@ -22,7 +22,7 @@ unmodified OQuPy TempoBackend from baseline/_ref when it is importable, else
 the plain-numpy port in oracle/) on a dkmax-stratified sample of the same
 batch, one single-threaded process per host core, and states the
 whole-trajectory throughput estimated from the measured prefixes.
-Other workloads: ``--workload pt | qutrit | surrogate``.
+Other workloads: ``--workload pt | qutrit | surrogate | heavy``.
 """
 
 import argparse
@@ -688,6 +688,49 @@ def _accuracy_vs_oracle(states, indices):
                               "oracle_envelope_max": r[3]} for r in rows]}
 
 
+def run_heavy(args):
+    """Critical-path instance: the late steps of the batch wait on their
+    longest instance, so time that instance alone.  The 512-instance batch
+    advances 60 steps in one launch; the instance with the largest
+    (window + 1) x bond^3 then runs alone on one CTA (512 threads, 200 KiB):
+    steps 1..N-1 in one launch, step N (``--heavy-steps``) in its own
+    launch, which is the third ``tempo_kernel`` launch of the process."""
+    import numpy as np
+    import torch
+    from oqupy_gb300.tempo import TempoBatch
+    N = int(args.heavy_steps)
+    insts = make_instances(args.instances, BATCH_SEED)
+    s = torch.cuda.current_stream()
+    b = TempoBatch(insts, precision="mixed", chi_cap=args.chi_cap, out_cap=2, block=512, smem_kb=200)
+    b.advance(60, s.cuda_stream)
+    torch.cuda.synchronize()
+    b.check_status()
+    bonds = [b.info(i)["max_bond"] for i in range(b.n)]
+    b.close()
+    cost = [(min(60, x["dkmax"]) + 1) * bonds[i] ** 3 for i, x in enumerate(insts)]
+    idx = int(np.argmax(cost))
+    h = TempoBatch([insts[idx]], precision="mixed", chi_cap=args.chi_cap, out_cap=N + 1,
+                   block=512, smem_kb=200)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(s)
+    h.advance(N - 1, s.cuda_stream)
+    ev[1].record(s)
+    ev[2].record(s)
+    h.advance(1, s.cuda_stream)
+    ev[3].record(s)
+    torch.cuda.synchronize()
+    h.check_status()
+    inf = h.info(0)
+    h.close()
+    print(json.dumps({"workload": "critical-path instance of the batched spin-boson configuration",
+                      "instance": idx, "dkmax": int(insts[idx]["dkmax"]), "step": int(inf["step"]),
+                      "max_bond": int(inf["max_bond"]),
+                      "ms_steps_before": ev[0].elapsed_time(ev[1]),
+                      "ms_last_step": ev[2].elapsed_time(ev[3]),
+                      "splits": int(inf["splits"]),
+                      "sweepsff_per_split": inf["sweeps32"] / max(1, inf["splits"])}))
+
+
 def tempo_workload_config(n, timed_steps):
     """The batched spin-boson workload's ``config`` (identical in both arms)."""
     return {"workload": (f"batched TEMPO spin-boson, {n} instances (alpha U[0.01,0.5], "
@@ -963,7 +1006,9 @@ def main():
     ap.add_argument("--smem-kb", type=int, default=0, help="dynamic shared memory per CTA (0 = default)")
     ap.add_argument("--qr-cut", type=float, default=0.0,
                     help="relative cut of the bond split's QR (0 = the precision form's default)")
-    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit"])
+    ap.add_argument("--workload", default="tempo", choices=["tempo", "surrogate", "pt", "qutrit", "heavy"])
+    ap.add_argument("--heavy-steps", type=int, default=120,
+                    help="heavy workload: the step of the critical-path instance that is timed alone")
     ap.add_argument("--qutrit-instances", type=int, default=128)
     ap.add_argument("--qutrit-chi-cap", type=int, default=96)
     ap.add_argument("--pt-instances", type=int, default=304)
@@ -1000,6 +1045,10 @@ def main():
                               "reported as cpu_baseline in the gb300 line"}))
             return
         run_pt(args)
+        return
+    if args.workload == "heavy":
+        if rank == 0 and args.impl != "reference":
+            run_heavy(args)
         return
     if args.workload == "surrogate":
         if rank != 0:

@@ -116,6 +116,11 @@ __device__ __forceinline__ void ffp_acc(float ah, float al, float bh, float bl, 
   sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+// A compensated accumulator (h, l) -- the exact leading terms through
+// two-sum in h, every rounding error and cross term in l (ffp_acc) -- as a
+// normalised double-float value.
+__device__ __forceinline__ ff ffacc_norm(float h, float l) { return two_sum(h, l); }
+
 __device__ __forceinline__ ccacc ccacc_zero() {
   ccacc a;
   a.xh = a.xl = a.yh = a.yl = 0.f;

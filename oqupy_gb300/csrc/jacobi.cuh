@@ -282,14 +282,20 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
         cff* ca = W + (size_t)a * ld;
         cff* cb = W + (size_t)b * ld;
         if (active) {
+          // gamma = u^H v as compensated accumulators (ffp_acc)
+          float grh = 0.f, grl = 0.f, gih = 0.f, gil = 0.f;
           for (int r = lane; r < m; r += G) {
             const cff u = ca[r];
             const cff v = cb[r];
             A = fmaf(u.x.hi, u.x.hi, fmaf(u.y.hi, u.y.hi, A));
             B = fmaf(v.x.hi, v.x.hi, fmaf(v.y.hi, v.y.hi, B));
-            gr = ff_fma(u.x, v.x, ff_fma(u.y, v.y, gr));
-            gi = ff_fma(u.x, v.y, ff_sub(gi, ff_mul(u.y, v.x)));
+            ffp_acc(u.x.hi, u.x.lo, v.x.hi, v.x.lo, grh, grl);
+            ffp_acc(u.y.hi, u.y.lo, v.y.hi, v.y.lo, grh, grl);
+            ffp_acc(u.x.hi, u.x.lo, v.y.hi, v.y.lo, gih, gil);
+            ffp_acc(-u.y.hi, -u.y.lo, v.x.hi, v.x.lo, gih, gil);
           }
+          gr = ffacc_norm(grh, grl);
+          gi = ffacc_norm(gih, gil);
         }
         for (int off = G >> 1; off > 0; off >>= 1) {
           A += __shfl_xor_sync(0xffffffffu, A, off, 32);
@@ -344,12 +350,30 @@ __device__ inline int jacobi_sweeps_ff(cff* W, int m, int n, int ld, JacobiShare
               const cff u = ca[r];
               const cff v = cb[r];
               cff nu, nv;
+              // each component one compensated accumulation of three products
+              float h, l;
               // nu = c u - q v
-              nu.x = ff_sub(ff_mul(fc, u.x), ff_sub(ff_mul(qx, v.x), ff_mul(qy, v.y)));
-              nu.y = ff_sub(ff_mul(fc, u.y), ff_add(ff_mul(qx, v.y), ff_mul(qy, v.x)));
+              h = l = 0.f;
+              ffp_acc(fc.hi, fc.lo, u.x.hi, u.x.lo, h, l);
+              ffp_acc(-qx.hi, -qx.lo, v.x.hi, v.x.lo, h, l);
+              ffp_acc(qy.hi, qy.lo, v.y.hi, v.y.lo, h, l);
+              nu.x = ffacc_norm(h, l);
+              h = l = 0.f;
+              ffp_acc(fc.hi, fc.lo, u.y.hi, u.y.lo, h, l);
+              ffp_acc(-qx.hi, -qx.lo, v.y.hi, v.y.lo, h, l);
+              ffp_acc(-qy.hi, -qy.lo, v.x.hi, v.x.lo, h, l);
+              nu.y = ffacc_norm(h, l);
               // nv = c v + w u, w = (qx, wy)
-              nv.x = ff_add(ff_mul(fc, v.x), ff_sub(ff_mul(qx, u.x), ff_mul(wy, u.y)));
-              nv.y = ff_add(ff_mul(fc, v.y), ff_add(ff_mul(qx, u.y), ff_mul(wy, u.x)));
+              h = l = 0.f;
+              ffp_acc(fc.hi, fc.lo, v.x.hi, v.x.lo, h, l);
+              ffp_acc(qx.hi, qx.lo, u.x.hi, u.x.lo, h, l);
+              ffp_acc(-wy.hi, -wy.lo, u.y.hi, u.y.lo, h, l);
+              nv.x = ffacc_norm(h, l);
+              h = l = 0.f;
+              ffp_acc(fc.hi, fc.lo, v.y.hi, v.y.lo, h, l);
+              ffp_acc(qx.hi, qx.lo, u.y.hi, u.y.lo, h, l);
+              ffp_acc(wy.hi, wy.lo, u.x.hi, u.x.lo, h, l);
+              nv.y = ffacc_norm(h, l);
               ca[r] = nu;
               cb[r] = nv;
             }

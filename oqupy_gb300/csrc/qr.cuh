@@ -75,6 +75,7 @@ struct QA<double> {
     wr = fma(a.x, x.x, fma(a.y, x.y, wr));
     wi = fma(a.x, x.y, fma(-a.y, x.x, wi));
   }
+  static __device__ __forceinline__ S fin(S v) { return v; }
   // x - a (bx + i by)
   static __device__ __forceinline__ E sub_scaled(const E& x, const E& a, S bx, S by) {
     return mk<double>(x.x - fma(a.x, bx, -a.y * by), x.y - fma(a.x, by, a.y * bx));
@@ -127,14 +128,27 @@ struct QA<ff> {
   static __device__ __forceinline__ S shfl(S v, int off) { return ff_shfl_xor(v, off); }
   static __device__ __forceinline__ S abs2_acc(const E& x, S acc) { return ff_fma(x.x, x.x, ff_fma(x.y, x.y, acc)); }
   static __device__ __forceinline__ float abs2f(const E& x) { return fmaf(x.x.hi, x.x.hi, x.y.hi * x.y.hi); }
+  // wr + i wi += conj(a) x as compensated accumulators (ffp_acc): the
+  // (hi, lo) pair is left unnormalised inside a loop; fin() normalises it
   static __device__ __forceinline__ void dotj(S& wr, S& wi, const E& a, const E& x) {
-    wr = ff_fma(a.x, x.x, ff_fma(a.y, x.y, wr));
-    wi = ff_fma(a.x, x.y, ff_sub(wi, ff_mul(a.y, x.x)));
+    ffp_acc(a.x.hi, a.x.lo, x.x.hi, x.x.lo, wr.hi, wr.lo);
+    ffp_acc(a.y.hi, a.y.lo, x.y.hi, x.y.lo, wr.hi, wr.lo);
+    ffp_acc(a.x.hi, a.x.lo, x.y.hi, x.y.lo, wi.hi, wi.lo);
+    ffp_acc(-a.y.hi, -a.y.lo, x.x.hi, x.x.lo, wi.hi, wi.lo);
   }
+  static __device__ __forceinline__ S fin(S v) { return ffacc_norm(v.hi, v.lo); }
+  // x - a (bx + i by), each component one compensated accumulation
   static __device__ __forceinline__ E sub_scaled(const E& x, const E& a, S bx, S by) {
     E r;
-    r.x = ff_sub(x.x, ff_sub(ff_mul(a.x, bx), ff_mul(a.y, by)));
-    r.y = ff_sub(x.y, ff_add(ff_mul(a.x, by), ff_mul(a.y, bx)));
+    float h = x.x.hi, l = x.x.lo;
+    ffp_acc(-a.x.hi, -a.x.lo, bx.hi, bx.lo, h, l);
+    ffp_acc(a.y.hi, a.y.lo, by.hi, by.lo, h, l);
+    r.x = ffacc_norm(h, l);
+    h = x.y.hi;
+    l = x.y.lo;
+    ffp_acc(-a.x.hi, -a.x.lo, by.hi, by.lo, h, l);
+    ffp_acc(-a.y.hi, -a.y.lo, bx.hi, bx.lo, h, l);
+    r.y = ffacc_norm(h, l);
     return r;
   }
   static __device__ __forceinline__ E conj(const E& x) {
@@ -311,6 +325,8 @@ __device__ int qrcp_inplace(typename QA<T>::E* X, int R, int N, float delta, flo
       if (act) {
         for (int r = i + gl; r < R; r += G) Q::dotj(wr, wi, (r == i) ? v0 : v[r], cj[r]);
       }
+      wr = Q::fin(wr);
+      wi = Q::fin(wi);
       for (int off = G >> 1; off > 0; off >>= 1) {
         wr = Q::add(wr, Q::shfl(wr, off));
         wi = Q::add(wi, Q::shfl(wi, off));
@@ -385,6 +401,8 @@ __device__ void householder_unit(typename QA<T>::E* Z, int M, int K, int ld, dou
       if (act) {
         for (int r = i + gl; r < M; r += G) Q::dotj(wr, wi, (r == i) ? v0 : v[r], cj[r]);
       }
+      wr = Q::fin(wr);
+      wi = Q::fin(wi);
       for (int off = G >> 1; off > 0; off >>= 1) {
         wr = Q::add(wr, Q::shfl(wr, off));
         wi = Q::add(wi, Q::shfl(wi, off));
@@ -428,6 +446,8 @@ __device__ void apply_q_unit(const typename QA<T>::E* Z, int M, int K, int ld, c
       if (act) {
         for (int r = i + gl; r < M; r += G) Q::dotj(sr, si, (r == i) ? one : w[r], y[r]);
       }
+      sr = Q::fin(sr);
+      si = Q::fin(si);
       for (int off = G >> 1; off > 0; off >>= 1) {
         sr = Q::add(sr, Q::shfl(sr, off));
         si = Q::add(si, Q::shfl(si, off));
