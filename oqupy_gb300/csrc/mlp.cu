@@ -138,6 +138,7 @@ __global__ void __launch_bounds__(TC_THREADS)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_err;
+  __shared__ int s_drain;  // phase parity of an MMA batch still in flight after a timed-out wait
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
 
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(TC_THREADS)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
     s_err = 0;
+    s_drain = -1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -167,7 +169,10 @@ __global__ void __launch_bounds__(TC_THREADS)
     if (kc >= 1) {
       // batch kc - 1 read the other buffer: wait for it before refilling, and
       // so that no more than one batch is outstanding at any parity wait
-      if (tid == 0 && !s_err && !tc_wait_phase(&mbar, (kc - 1) & 1)) s_err = 1;
+      if (tid == 0 && !s_err && !tc_wait_phase(&mbar, (kc - 1) & 1)) {
+        s_err = 1;
+        s_drain = (kc - 1) & 1;
+      }
       asm volatile("tcgen05.fence::after_thread_sync;");
       __syncthreads();
       if (s_err) break;
@@ -200,7 +205,10 @@ __global__ void __launch_bounds__(TC_THREADS)
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   // the last committed batch: every earlier one was waited for in the loop
-  if (tid == 0 && !s_err && issued > 0 && !tc_wait_phase(&mbar, (issued - 1) & 1)) s_err = 1;
+  if (tid == 0 && !s_err && issued > 0 && !tc_wait_phase(&mbar, (issued - 1) & 1)) {
+    s_err = 1;
+    s_drain = (issued - 1) & 1;
+  }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
@@ -238,6 +246,9 @@ __global__ void __launch_bounds__(TC_THREADS)
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
+    // one more bounded wait for the batch still in flight, so that it is
+    // not writing the accumulator when the columns are released
+    if (s_drain >= 0) tc_wait_phase(&mbar, s_drain);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -257,6 +268,7 @@ __global__ void __launch_bounds__(TC_THREADS)
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_err;
+  __shared__ int s_drain;  // phase parity of an MMA batch still in flight after a timed-out wait
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
 
@@ -269,6 +281,7 @@ __global__ void __launch_bounds__(TC_THREADS)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
     s_err = 0;
+    s_drain = -1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -307,7 +320,10 @@ __global__ void __launch_bounds__(TC_THREADS)
           : "=r"(done)
           : "r"(smem_u32(&mbar)), "r"(phase));
     }
-    if (!done) s_err = 1;
+    if (!done) {
+      s_err = 1;
+      s_drain = phase;
+    }
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
     __syncthreads();
@@ -347,6 +363,9 @@ __global__ void __launch_bounds__(TC_THREADS)
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
+    // one more bounded wait for the batch still in flight, so that it is
+    // not writing the accumulator when the columns are released
+    if (s_drain >= 0) tc_wait_phase(&mbar, s_drain);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
