@@ -238,6 +238,25 @@ otb_status otb_dyn_run_steps(otb_pt* h, int32_t inst, int32_t n_systems,
                              const int32_t* prop_index, const double* rho0,
                              int32_t num_steps, double* out, void* stream);
 
+/* The forward and adjoint sweeps of compute_gradient_and_dynamics
+ * (gradient.py:169-437) for n_systems systems on one process tensor, with
+ * propagator pairs as in otb_dyn_run_steps.  num_steps must end where the
+ * process tensor's bond closes (its full length).  out_states receives
+ * (num_steps+1) * n_systems * D complex (the dynamics); out_cores
+ * n_systems * num_steps * D^3 complex: per step n the core
+ * C[a][m][e] = sum_{l,r} v_n[l][a] T_n[l][r][m] Y_{n+1}[r][e] of the
+ * derivative tensor, v_n the state with its bond leg at the start of step n
+ * and Y_{n+1} the adjoint vector (the target swept back through steps
+ * num_steps-1 .. n+1); the reference's tensor follows on the host by
+ * applying the post-measurement control of step n to leg a, the transposed
+ * pre-measurement control of step n+1 to leg e and the process tensor's
+ * transforms to leg m. */
+otb_status otb_dyn_gradient(otb_pt* h, int32_t inst, int32_t n_systems,
+                            const double* props, int32_t n_props,
+                            const int32_t* prop_index, const double* rho0,
+                            const double* target, int32_t num_steps,
+                            double* out_states, double* out_cores, void* stream);
+
 /* ----------------------------------------------- allocation-free TEMPO */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -55,18 +55,11 @@ class PropagatorTable:
         return len(self._rows)
 
 
-def device_dynamics(process_tensor, propagators: Sequence[Callable[[int], Tuple]],
-                    initial_states: Sequence[np.ndarray], num_steps: int,
-                    controls: Optional[Sequence[Optional[Dict]]] = None) -> np.ndarray:
-    """``compute_dynamics`` of several systems on one device process tensor
-    in one batched sweep.
-
-    ``propagators[h](step) -> (P1, P2)`` (``BaseSystem.get_propagators``'s
-    function; slots that share one function object share its pairs);
-    ``controls[h]``: ``None`` or ``{"pre": {step: C}, "post": {step: C}}``
-    superoperators.  Returns states ``[num_steps+1, H, D]`` (the state of
-    every step, read after that step's pre-measurement control).
-    """
+def propagator_table(process_tensor, propagators, initial_states, num_steps, controls=None):
+    """The sweep inputs of several systems: ``(batch, index in the batch,
+    pair table [n_props, 2, D, D], pair index [H, num_steps], rho0 [H, D])``
+    with the process tensor's transforms and the control operations folded
+    in (see the module docstring)."""
     batch, i, tin, tout = _pt_handle(process_tensor)
     H = len(initial_states)
     n = int(num_steps)
@@ -106,12 +99,61 @@ def device_dynamics(process_tensor, propagators: Sequence[Callable[[int], Tuple]
                     p2 = np.asarray(pre[k + 1]) @ p2
                 index[h, k] = table.add(p1, p2)
         rho0.append(rho)
-    rho0 = np.array(rho0)
+    return batch, i, table.array(), index, np.array(rho0)
+
+
+def device_dynamics(process_tensor, propagators: Sequence[Callable[[int], Tuple]],
+                    initial_states: Sequence[np.ndarray], num_steps: int,
+                    controls: Optional[Sequence[Optional[Dict]]] = None) -> np.ndarray:
+    """``compute_dynamics`` of several systems on one device process tensor
+    in one batched sweep.
+
+    ``propagators[h](step) -> (P1, P2)`` (``BaseSystem.get_propagators``'s
+    function; slots that share one function object share its pairs);
+    ``controls[h]``: ``None`` or ``{"pre": {step: C}, "post": {step: C}}``
+    superoperators.  Returns states ``[num_steps+1, H, D]`` (the state of
+    every step, read after that step's pre-measurement control).
+    """
+    batch, i, table, index, rho0 = propagator_table(process_tensor, propagators, initial_states,
+                                                    num_steps, controls)
+    H = len(rho0)
     out = []
     for s in range(0, H, MAX_SLOTS):
-        out.append(batch.dynamics_steps(i, table.array(), index[s:s + MAX_SLOTS],
-                                        rho0[s:s + MAX_SLOTS], n))
+        out.append(batch.dynamics_steps(i, table, index[s:s + MAX_SLOTS], rho0[s:s + MAX_SLOTS],
+                                        int(num_steps)))
     return np.concatenate(out, axis=1)
+
+
+def device_gradient(process_tensor, propagators: Callable[[int], Tuple], initial_state: np.ndarray,
+                    target: np.ndarray, num_steps: int, controls: Optional[Dict] = None):
+    """``compute_gradient_and_dynamics`` (gradient.py:169-437) on one device
+    process tensor: the forward sweep keeps the state with its bond leg at
+    every step, the adjoint sweep carries the target back through the
+    transposed steps, and a kernel contracts both with every step's
+    process-tensor tensor (``otb_dyn_gradient``).  The controls and
+    transforms act on the outer legs of each step's tensor and are applied
+    here.  Returns ``(derivs[num_steps, D, D, D, D], states[num_steps+1, D])``
+    in the reference's leg order: [0] the state leg before the first
+    half-step propagator of step n, [1] / [2] the MPO's input / output legs,
+    [3] the leg after the second half-step propagator."""
+    batch, i, tin, tout = _pt_handle(process_tensor)
+    _, _, table, index, rho0 = propagator_table(process_tensor, [propagators], [initial_state],
+                                                num_steps, [controls])
+    n = int(num_steps)
+    D = rho0.shape[1]
+    states, cores = batch.gradient_cores(i, table, index, rho0, np.asarray(target).reshape(1, D), n)
+    core = cores[0]                                   # [n, a', m, e']
+    pre = (controls or {}).get("pre", {})
+    post = (controls or {}).get("post", {})
+    eye = np.identity(D, dtype=np.complex128)
+    Tin = eye if tin is None else np.asarray(tin, dtype=np.complex128)
+    Tout = eye if tout is None else np.asarray(tout, dtype=np.complex128)
+    derivs = np.empty((n, D, D, D, D), dtype=np.complex128)
+    for k in range(n):
+        Pa = np.asarray(post.get(k, eye))             # F_k = post_k v_k on leg a
+        Pe = np.asarray(pre.get(k + 1, eye))          # B_{k+1} = pre_{k+1}^T Y_{k+1} on leg e
+        derivs[k] = np.einsum("ax,bm,mc,ye,xmy->abce", Pa, Tin, Tout, Pe, core[k])
+    return derivs, states[:, 0]
 
 
 def superoperator(operator: np.ndarray, side: str) -> np.ndarray:

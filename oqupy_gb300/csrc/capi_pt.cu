@@ -319,6 +319,10 @@ static otb_status dyn_run_impl(otb_pt* h, int32_t inst, int32_t nh, const double
   L.counter = (unsigned int*)dcnt.p;
   L.max_chunks = max_chunks;
   L.k = 0;
+  L.fwd_hist = nullptr;
+  L.back_hist = nullptr;
+  L.deriv = nullptr;
+  L.hist_steps = 0;
   if (!check_cuda(launch_dyn_init(L, (const double*)drho.p, s), "dyn init")) return OTB_ERR_CUDA;
   // the whole sweep as one CUDA graph: one kernel node per step
   cudaStream_t cs;
@@ -352,6 +356,98 @@ static otb_status dyn_run_impl(otb_pt* h, int32_t inst, int32_t nh, const double
   cudaEventDestroy(ready);
   cudaStreamDestroy(cs);
   return ok ? OTB_OK : OTB_ERR_CUDA;
+}
+
+extern "C" otb_status otb_dyn_gradient(otb_pt* h, int32_t inst, int32_t nh, const double* props,
+                                       int32_t n_props, const int32_t* prop_index, const double* rho0,
+                                       const double* target, int32_t num_steps, double* out_states,
+                                       double* out_cores, void* stream) {
+  otb_status st = pt_check(h, inst);
+  if (st) return st;
+  const PtDev& I = h->inst[inst];
+  if (!props || !prop_index || !rho0 || !target || !out_states || !out_cores || nh < 1 || nh > 1024 ||
+      num_steps < 1 || num_steps > I.num_steps || n_props < 1)
+    return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  for (long long e = 0; e < (long long)nh * num_steps; ++e)
+    if (prop_index[e] < 0 || prop_index[e] >= n_props)
+      return set_error(OTB_ERR_INVALID_ARG, "propagator index out of range");
+  if ((st = pt_refresh(h, inst))) return st;
+  if (!h->state[inst].caps_done) return set_error(OTB_ERR_INVALID_ARG, "process tensor not complete");
+  std::vector<int2> dims;
+  if ((st = pt_dims(h, inst, dims))) return st;
+  // the target carries no bond: the sweep must end where the process tensor's bond closes
+  if (dims[num_steps - 1].y != 1)
+    return set_error(OTB_ERR_INVALID_ARG, "gradient needs num_steps = the process tensor's length (closed bond)");
+  int max_r = 1;
+  for (int k = 0; k < num_steps; ++k) max_r = std::max(max_r, std::max(dims[k].x, dims[k].y));
+  const int D = I.D;
+  const size_t tb = (size_t)n_props * 2 * D * D * 16, vb = (size_t)nh * I.cap * D * 16;
+  const size_t ib = (size_t)nh * num_steps * sizeof(int32_t);
+  const size_t ob = (size_t)(num_steps + 1) * nh * D * 16;
+  const size_t fb = (size_t)nh * num_steps * I.cap * D * 16;
+  const size_t bb = (size_t)nh * (num_steps + 1) * I.cap * D * 16;
+  const size_t cb = (size_t)nh * num_steps * D * D * D * 16;
+  const int max_chunks = (I.cap + 31) / 32;
+  DevBuf dtab, didx, drho, dtgt, dv0, dv1, dout, dpart, dcnt, dfwd, dback, dcore;
+  if (!dtab.alloc(tb) || !didx.alloc(ib) || !drho.alloc((size_t)nh * D * 16) ||
+      !dtgt.alloc((size_t)nh * D * 16) || !dv0.alloc(vb) || !dv1.alloc(vb) || !dout.alloc(ob) ||
+      !dpart.alloc((size_t)nh * max_chunks * D * 16) || !dcnt.alloc((size_t)nh * sizeof(unsigned int)) ||
+      !dfwd.alloc(fb) || !dback.alloc(bb) || !dcore.alloc(cb))
+    return OTB_ERR_OOM;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!check_cuda(cudaMemcpyAsync(dtab.p, props, tb, cudaMemcpyHostToDevice, s), "upload") ||
+      !check_cuda(cudaMemcpyAsync(didx.p, prop_index, ib, cudaMemcpyHostToDevice, s), "upload") ||
+      !check_cuda(cudaMemcpyAsync(drho.p, rho0, (size_t)nh * D * 16, cudaMemcpyHostToDevice, s), "upload") ||
+      !check_cuda(cudaMemcpyAsync(dtgt.p, target, (size_t)nh * D * 16, cudaMemcpyHostToDevice, s), "upload") ||
+      !check_cuda(cudaMemsetAsync(dout.p, 0, ob, s), "memset") ||
+      !check_cuda(cudaMemsetAsync(dv0.p, 0, vb, s), "memset") ||
+      !check_cuda(cudaMemsetAsync(dfwd.p, 0, fb, s), "memset") ||
+      !check_cuda(cudaMemsetAsync(dback.p, 0, bb, s), "memset") ||
+      !check_cuda(cudaMemsetAsync(dcnt.p, 0, (size_t)nh * sizeof(unsigned int), s), "memset"))
+    return OTB_ERR_CUDA;
+  DynLaunch L;
+  L.nh = nh;
+  L.D = D;
+  L.d = I.d;
+  L.sites = (const double*)h->d_sites.p + 2 * I.site_base;
+  L.slot_elems = (long long)I.cap * D * I.cap;
+  L.dims = (const int2*)h->d_dims.p + I.dims_base;
+  L.caps = (const double*)h->d_caps.p + 2 * I.caps_base;
+  L.cap = I.cap;
+  L.ptab = (const double*)dtab.p;
+  L.pidx = (const int*)didx.p;
+  L.pidx_stride = num_steps;
+  L.vcur = (double*)dv0.p;
+  L.vnext = (double*)dv1.p;
+  L.out = (double*)dout.p;
+  L.partial = (double*)dpart.p;
+  L.counter = (unsigned int*)dcnt.p;
+  L.max_chunks = max_chunks;
+  L.k = 0;
+  L.fwd_hist = (double*)dfwd.p;
+  L.back_hist = (double*)dback.p;
+  L.deriv = (double*)dcore.p;
+  L.hist_steps = num_steps;
+  if (!check_cuda(launch_dyn_init(L, (const double*)drho.p, s), "dyn init")) return OTB_ERR_CUDA;
+  for (int k = 0; k < num_steps; ++k) {
+    DynLaunch Lk = L;
+    Lk.k = k;
+    Lk.vcur = (k % 2 == 0) ? (double*)dv0.p : (double*)dv1.p;
+    Lk.vnext = (k % 2 == 0) ? (double*)dv1.p : (double*)dv0.p;
+    if (!check_cuda(launch_dyn_step(Lk, dims[k].y, s), "forward step")) return OTB_ERR_CUDA;
+  }
+  if (!check_cuda(launch_dyn_back_init(L, (const double*)dtgt.p, s), "adjoint init")) return OTB_ERR_CUDA;
+  for (int k = num_steps - 1; k >= 1; --k) {
+    DynLaunch Lk = L;
+    Lk.k = k;
+    if (!check_cuda(launch_dyn_back_step(Lk, dims[k].x, dims[k].y, s), "adjoint step")) return OTB_ERR_CUDA;
+  }
+  if (!check_cuda(launch_dyn_deriv(L, num_steps, max_r, s), "derivative cores")) return OTB_ERR_CUDA;
+  if (!check_cuda(cudaMemcpyAsync(out_states, dout.p, ob, cudaMemcpyDeviceToHost, s), "download") ||
+      !check_cuda(cudaMemcpyAsync(out_cores, dcore.p, cb, cudaMemcpyDeviceToHost, s), "download") ||
+      !check_cuda(cudaStreamSynchronize(s), "sync"))
+    return OTB_ERR_CUDA;
+  return OTB_OK;
 }
 
 extern "C" otb_status otb_dyn_run(otb_pt* h, int32_t inst, int32_t nh, const double* p1, const double* p2,

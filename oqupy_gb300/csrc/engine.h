@@ -147,9 +147,17 @@ struct DynLaunch {
   unsigned int* counter;  // nh counters of finished chunks (zero between steps)
   int max_chunks;
   int k;                // step
+  // gradient sweeps (otb_dyn_gradient; null / unused otherwise)
+  double* fwd_hist;     // nh * hist_steps * cap * D: v_k at the start of step k
+  double* back_hist;    // nh * (hist_steps + 1) * cap * D: adjoint vectors Y_k
+  double* deriv;        // nh * hist_steps * D^3: per-step derivative cores
+  int hist_steps;
 };
 
 cudaError_t launch_dyn_step(const DynLaunch& L, int r, cudaStream_t stream);
 cudaError_t launch_dyn_init(const DynLaunch& L, const double* rho0, cudaStream_t stream);
+cudaError_t launch_dyn_back_init(const DynLaunch& L, const double* target, cudaStream_t stream);
+cudaError_t launch_dyn_back_step(const DynLaunch& L, int l, int r, cudaStream_t stream);
+cudaError_t launch_dyn_deriv(const DynLaunch& L, int num_steps, int max_r, cudaStream_t stream);
 
 }  // namespace otb

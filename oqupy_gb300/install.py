@@ -27,7 +27,9 @@ first copied to a host ``SimpleProcessTensor``).  Both
 ``oqupy.system_dynamics.compute_dynamics`` and ``oqupy.compute_dynamics``
 (bound at import, oqupy/__init__.py:104) are rebound, and so is
 ``compute_correlations_nt`` (which ``compute_correlations`` calls): on a
-device process tensor its runs become the slots of one batched sweep.
+device process tensor its runs become the slots of one batched sweep; and
+``oqupy.gradient.compute_gradient_and_dynamics`` (which ``state_gradient``
+calls), whose forward and adjoint sweeps run on the GPU.
 """
 
 from typing import Any, Dict, Optional
@@ -241,6 +243,54 @@ def install(oqupy_module: Any = None) -> None:
         if _installed["compute_correlations_nt_pkg"] is not None:
             oqupy_module.compute_correlations_nt = compute_correlations_nt
 
+        # compute_gradient_and_dynamics (oqupy/gradient.py:169-437; reached
+        # through state_gradient): on one device process tensor, the forward
+        # and adjoint sweeps run on the GPU
+        grad_mod = importlib.import_module(oqupy_module.__name__ + ".gradient")
+        ref_grad = grad_mod.compute_gradient_and_dynamics
+        _installed["compute_gradient_and_dynamics"] = ref_grad
+
+        def compute_gradient_and_dynamics(system, initial_state, target_derivative, process_tensors,
+                                          parameters, start_time=0.0, dt=None, num_steps=None,
+                                          control=None, record_all=True, progress_type=None):
+            pts = process_tensors if isinstance(process_tensors, list) else [process_tensors]
+            if not (len(pts) == 1 and isinstance(pts[0], dev_cls) and record_all):
+                hosts = [host_copy(p) for p in pts]
+                return ref_grad(system, initial_state, target_derivative,
+                                hosts if isinstance(process_tensors, list) else hosts[0], parameters,
+                                start_time=start_time, dt=dt, num_steps=num_steps, control=control,
+                                record_all=record_all, progress_type=progress_type)
+            parsed = sd_mod._compute_dynamics_input_parse(
+                False, system, initial_state, dt, num_steps, start_time,
+                process_tensors, control, record_all)
+            system, initial_state, dt, num_steps, start_time = parsed[:5]
+            hs_dim = parsed[-1]
+            props = system.get_propagators(dt, parameters)
+            ctl = None
+            if control is not None:
+                ctl = {"pre": {}, "post": {}}
+                for step in range(num_steps + 1):
+                    pre, post = control.get_controls(step, dt=dt, start_time=start_time)
+                    if pre is not None:
+                        ctl["pre"][step] = pre
+                    if post is not None:
+                        ctl["post"][step] = post
+            from . import correlations as corr
+            rho0 = initial_state.reshape(-1)
+            target = target_derivative
+            if callable(target):
+                # the reference evaluates it on the final state (gradient.py:350-351)
+                st = corr.device_dynamics(pts[0], [props], [rho0], num_steps, [ctl])
+                target = target(st[-1, 0].reshape(hs_dim, hs_dim))
+            derivs, states = corr.device_gradient(pts[0], props, rho0, np.asarray(target).reshape(-1),
+                                                  num_steps, ctl)
+            mats = [s.reshape(hs_dim, hs_dim) for s in states]
+            times = start_time + np.arange(len(mats)) * dt
+            return list(derivs), dyn_mod.Dynamics(times=list(times), states=mats)
+
+        compute_gradient_and_dynamics.reference_function = ref_grad
+        grad_mod.compute_gradient_and_dynamics = compute_gradient_and_dynamics
+
 
 def uninstall(oqupy_module: Any = None) -> None:
     if oqupy_module is None:
@@ -263,6 +313,8 @@ def uninstall(oqupy_module: Any = None) -> None:
         if pkg is not None:
             oqupy_module.compute_dynamics = pkg
         sd_mod.compute_correlations_nt = _installed.pop("compute_correlations_nt")
+        grad_mod = importlib.import_module(oqupy_module.__name__ + ".gradient")
+        grad_mod.compute_gradient_and_dynamics = _installed.pop("compute_gradient_and_dynamics")
         pkg = _installed.pop("compute_correlations_nt_pkg", None)
         if pkg is not None:
             oqupy_module.compute_correlations_nt = pkg

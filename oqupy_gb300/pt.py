@@ -171,6 +171,27 @@ class PtBatch:
             nat.dptr(out), ctypes.c_void_p(stream or 0)))
         return out.view(np.complex128)[..., 0]
 
+    def gradient_cores(self, i: int, props, prop_index, rho0, target, num_steps: int,
+                       stream: Optional[int] = None):
+        """Forward and adjoint sweeps of the gradient (``otb_dyn_gradient``)
+        for ``H`` systems: ``props`` ``[n_props, 2, D, D]``, ``prop_index``
+        ``[H, num_steps]``, ``rho0`` and ``target`` ``[H, D]``.  Returns
+        ``(states[num_steps+1, H, D], cores[H, num_steps, D, D, D])``."""
+        D = self.meta[i]["D"]
+        tab = nat.cplx(np.asarray(props, dtype=np.complex128).reshape(-1, 2, D, D))
+        n = int(num_steps)
+        r0a = np.asarray(rho0, dtype=np.complex128).reshape(-1, D)
+        H = r0a.shape[0]
+        idx = np.ascontiguousarray(np.asarray(prop_index, dtype=np.int32).reshape(H, n))
+        tg = nat.cplx(np.asarray(target, dtype=np.complex128).reshape(H, D))
+        states = np.zeros((n + 1, H, D, 2))
+        cores = np.zeros((H, n, D, D, D, 2))
+        nat.check(nat.lib().otb_dyn_gradient(
+            self._h, int(i), H, nat.dptr(tab), int(tab.shape[0]),
+            idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nat.dptr(nat.cplx(r0a)), nat.dptr(tg),
+            n, nat.dptr(states), nat.dptr(cores), ctypes.c_void_p(stream or 0)))
+        return states.view(np.complex128)[..., 0], cores.view(np.complex128)[..., 0]
+
 
 class GpuPtTempoBackend:
     """Drop-in for ``oqupy.backends.pt_tempo_backend.PtTempoBackend``

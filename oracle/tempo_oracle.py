@@ -24,6 +24,8 @@ Reference being restated (OQuPy 0.5.0, paths relative to the project root):
 * ``oqupy/backends/pt_tempo_backend.py:105-316`` ``PtTempoBackend``
 * ``oqupy/process_tensor.py:326-406``  ``get_mpo_tensor`` / ``compute_caps``
 * ``oqupy/system_dynamics.py:41-182, 631-700``  ``compute_dynamics``
+* ``oqupy/system_dynamics.py:791-990``  ``compute_correlations_nt``
+* ``oqupy/gradient.py:169-437``  ``compute_gradient_and_dynamics``
 * truncation rule of ``tensornetwork.split_node_full_svd(relative=True)``,
   also stated in-tree at ``oqupy/mps_mpo.py:452-457``.
 """
@@ -537,6 +539,62 @@ def compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps,
         v = v @ np.asarray(p2, CDT).T
     states.append(np.einsum("ba,b->a", v, caps[num_steps]))
     return np.array(states)
+
+
+def gradient_pt(initial_state, propagators, mpo_tensors, caps, num_steps, target,
+                transform_in=None, transform_out=None, controls=None):
+    """``compute_gradient_and_dynamics`` with one process tensor
+    (gradient.py:169-437; helpers system_dynamics.py:631-790).  Forward: the
+    sweep of ``compute_dynamics_pt``, keeping the node after every step's
+    post-measurement control (the forward derivative tensor ``F_n[l, a]``).
+    Backward: the target (a ``D`` vector, bond 1) through the step's
+    pre-measurement control transposed, then per step N-1 .. 1 through
+    ``P2^T``, the MPO with bond and system legs swapped, ``P1^T`` and the
+    post- and pre-measurement controls transposed (``B_n[r, e]``).  Returns
+    ``(derivs[num_steps, D, D, D, D], states[num_steps+1, D])`` with
+    ``derivs[n][a, b, c, e] = sum_{l, r} F_n[l, a] MPO_n[l, r, b, c]
+    B_{n+1}[r, e]``: the derivative of the target's overlap with respect to
+    the half-step propagators around the MPO of step n."""
+    rho = np.asarray(initial_state, dtype=CDT).reshape(-1)
+    D = rho.size
+    ctl = controls if controls is not None else (lambda s: (None, None))
+    v = rho.reshape(1, D)
+    states, fwd, mpos = [], [], []
+    for step in range(num_steps + 1):
+        pre, post = ctl(step)
+        if pre is not None:
+            v = v @ np.asarray(pre, CDT).T
+        if step == num_steps:
+            break
+        states.append(np.einsum("ba,b->a", v, caps[step]))
+        if post is not None:
+            v = v @ np.asarray(post, CDT).T
+        fwd.append(v.copy())
+        p1, p2 = propagators(step)
+        T = pt_mpo_rank4(mpo_tensors[step], transform_in, transform_out)
+        mpos.append(T)
+        v = v @ np.asarray(p1, CDT).T
+        v = np.einsum("la,lrab->rb", v, T)
+        v = v @ np.asarray(p2, CDT).T
+    states.append(np.einsum("ba,b->a", v, caps[num_steps]))
+    b = np.asarray(target, dtype=CDT).reshape(1, D)
+    pre, _ = ctl(num_steps)
+    if pre is not None:
+        b = b @ np.asarray(pre, CDT)          # (pre^T b) as a row vector
+    derivs = [None] * num_steps
+    derivs[num_steps - 1] = np.einsum("la,lrbc,re->abce", fwd[num_steps - 1], mpos[num_steps - 1], b)
+    for step in range(num_steps - 1, 0, -1):
+        pre, post = ctl(step)
+        p1, p2 = propagators(step)
+        b = b @ np.asarray(p2, CDT)           # P2^T
+        b = np.einsum("re,lrbe->lb", b, mpos[step])
+        b = b @ np.asarray(p1, CDT)           # P1^T
+        if post is not None:
+            b = b @ np.asarray(post, CDT)
+        if pre is not None:
+            b = b @ np.asarray(pre, CDT)
+        derivs[step - 1] = np.einsum("la,lrbc,re->abce", fwd[step - 1], mpos[step - 1], b)
+    return np.array(derivs), np.array(states)
 
 
 def correlations_nt_pt(initial_state, propagators, mpo_tensors, caps, operators,
