@@ -29,7 +29,7 @@ def test_gpu_gradient_matches_reference(name, tag, precision):
     d = int(g[f"{name}/d"])
     b = PtBatch([dict(hs_dim=d, num_steps=int(g[f"{name}/nsteps"]), dkmax=int(g[f"{name}/dkmax"]),
                       epsrel=float(g[f"{name}/epsrel"]), influences=g[f"{name}/influences"])],
-                precision=precision, chi_cap=64)
+                precision=precision, chi_cap=1152 // (d * d))
     b.build()
 
     class Pt:
