@@ -238,6 +238,22 @@ otb_status otb_dyn_run_steps(otb_pt* h, int32_t inst, int32_t n_systems,
                              const int32_t* prop_index, const double* rho0,
                              int32_t num_steps, double* out, void* stream);
 
+/* A sweep advanced one step per call (compute_dynamics_with_field,
+ * system_dynamics.py:184-476, where each step's propagators depend on a
+ * field computed from the states so far).  create: n_systems slots on
+ * process tensor inst (which must outlive the session), rho0 n_systems * D
+ * complex.  step: props holds this step's n_systems pairs (P1 then P2, D * D
+ * complex each, transforms and controls folded in as for otb_dyn_run_steps);
+ * state_out receives the n_systems * D states after the step.  state: the
+ * states of an earlier step (0 .. steps done). */
+typedef struct otb_dyn_session otb_dyn_session;
+otb_status otb_dyn_session_create(otb_pt* h, int32_t inst, int32_t n_systems,
+                                  const double* rho0, otb_dyn_session** out);
+otb_status otb_dyn_session_step(otb_dyn_session* s, const double* props,
+                                double* state_out, void* stream);
+otb_status otb_dyn_session_state(otb_dyn_session* s, int32_t step, double* state_out);
+void otb_dyn_session_destroy(otb_dyn_session* s);
+
 /* The forward and adjoint sweeps of compute_gradient_and_dynamics
  * (gradient.py:169-437) for n_systems systems on one process tensor, with
  * propagator pairs as in otb_dyn_run_steps.  num_steps must end where the

@@ -127,6 +127,10 @@ def _declare(lib):
                                     c_double_p, P]),
         "otb_dyn_gradient": (i32, [P, i32, i32, c_double_p, i32, c_int32_p, c_double_p, c_double_p,
                                    i32, c_double_p, c_double_p, P]),
+        "otb_dyn_session_create": (i32, [P, i32, i32, c_double_p, ctypes.POINTER(P)]),
+        "otb_dyn_session_step": (i32, [P, c_double_p, c_double_p, P]),
+        "otb_dyn_session_state": (i32, [P, i32, c_double_p]),
+        "otb_dyn_session_destroy": (None, [P]),
         "otb_mlp_gemm": (i32, [P, P, i32, i32, i32, P, i32, P, P, P, P, P, P]),
         "otb_mlp_transpose_bf16": (i32, [P, P, i32, i32, P]),
         "otb_mlp_f32_to_bf16": (i32, [P, P, ctypes.c_int64, P]),
@@ -156,7 +160,8 @@ def exported_symbols():
         "otb_tempo_set_propagators", "otb_tempo_set_all_propagators", "otb_tempo_set_first_influence",
         "otb_tempo_reserve_sites", "otb_tempo_set_launch", "otb_pt_create", "otb_pt_destroy",
         "otb_pt_advance", "otb_pt_get_info", "otb_pt_bond_dims",
-        "otb_pt_get_tensor", "otb_pt_get_cap", "otb_dyn_run", "otb_dyn_run_steps", "otb_dyn_gradient", "otb_mlp_gemm",
+        "otb_pt_get_tensor", "otb_pt_get_cap", "otb_dyn_run", "otb_dyn_run_steps", "otb_dyn_gradient", "otb_dyn_session_create",
+        "otb_dyn_session_step", "otb_dyn_session_state", "otb_dyn_session_destroy", "otb_mlp_gemm",
         "otb_mlp_transpose_bf16", "otb_mlp_f32_to_bf16", "otb_mlp_colsum",
         "otb_mlp_mse_grad", "otb_mlp_adamw", "otb_mlp_bloch_free_add",
         "otb_measure_fma_peak", "otb_last_error", "otb_version"]

@@ -358,6 +358,122 @@ static otb_status dyn_run_impl(otb_pt* h, int32_t inst, int32_t nh, const double
   return ok ? OTB_OK : OTB_ERR_CUDA;
 }
 
+// A sweep advanced one step per call, for callers that choose each step's
+// propagators from the states so far (compute_dynamics_with_field,
+// system_dynamics.py:184-476): the device keeps the states with their bond
+// legs between calls.  The process tensor must outlive the session.
+struct otb_dyn_session {
+  otb_pt* pt = nullptr;
+  int inst = 0;
+  int nh = 0;
+  int k = 0;            // steps done
+  int num_steps = 0;    // the process tensor's length
+  std::vector<int2> dims;
+  DevBuf dtab, didx, dv0, dv1, dout, dpart, dcnt;
+};
+
+extern "C" otb_status otb_dyn_session_create(otb_pt* h, int32_t inst, int32_t nh, const double* rho0,
+                                             otb_dyn_session** out) {
+  if (!out) return set_error(OTB_ERR_INVALID_ARG, "null output");
+  *out = nullptr;
+  otb_status st = pt_check(h, inst);
+  if (st) return st;
+  if (!rho0 || nh < 1 || nh > 1024) return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  if ((st = pt_refresh(h, inst))) return st;
+  if (!h->state[inst].caps_done) return set_error(OTB_ERR_INVALID_ARG, "process tensor not complete");
+  std::unique_ptr<otb_dyn_session> ss(new otb_dyn_session());
+  ss->pt = h;
+  ss->inst = inst;
+  ss->nh = nh;
+  const PtDev& I = h->inst[inst];
+  ss->num_steps = I.num_steps;
+  if ((st = pt_dims(h, inst, ss->dims))) return st;
+  const int D = I.D;
+  const size_t vb = (size_t)nh * I.cap * D * 16;
+  const size_t ob = (size_t)(I.num_steps + 1) * nh * D * 16;
+  const int max_chunks = (I.cap + 31) / 32;
+  if (!ss->dtab.alloc((size_t)nh * 2 * D * D * 16) || !ss->didx.alloc((size_t)nh * I.num_steps * sizeof(int32_t)) ||
+      !ss->dv0.alloc(vb) || !ss->dv1.alloc(vb) || !ss->dout.alloc(ob) ||
+      !ss->dpart.alloc((size_t)nh * max_chunks * D * 16) || !ss->dcnt.alloc((size_t)nh * sizeof(unsigned int)))
+    return OTB_ERR_OOM;
+  // system h always uses pair h of the table, which every step replaces
+  std::vector<int32_t> idx((size_t)nh * I.num_steps);
+  for (int i = 0; i < nh; ++i)
+    for (int k = 0; k < I.num_steps; ++k) idx[(size_t)i * I.num_steps + k] = i;
+  DevBuf drho;
+  if (!drho.alloc((size_t)nh * D * 16)) return OTB_ERR_OOM;
+  if (!check_cuda(cudaMemcpy(ss->didx.p, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
+                  "upload") ||
+      !check_cuda(cudaMemcpy(drho.p, rho0, (size_t)nh * D * 16, cudaMemcpyHostToDevice), "upload") ||
+      !check_cuda(cudaMemset(ss->dout.p, 0, ob), "memset") || !check_cuda(cudaMemset(ss->dv0.p, 0, vb), "memset") ||
+      !check_cuda(cudaMemset(ss->dcnt.p, 0, (size_t)nh * sizeof(unsigned int)), "memset"))
+    return OTB_ERR_CUDA;
+  DynLaunch L{};
+  L.nh = nh;
+  L.D = D;
+  L.d = I.d;
+  L.caps = (const double*)h->d_caps.p + 2 * I.caps_base;
+  L.vcur = (double*)ss->dv0.p;
+  L.out = (double*)ss->dout.p;
+  if (!check_cuda(launch_dyn_init(L, (const double*)drho.p, 0), "dyn init") ||
+      !check_cuda(cudaDeviceSynchronize(), "sync"))
+    return OTB_ERR_CUDA;
+  *out = ss.release();
+  return OTB_OK;
+}
+
+extern "C" otb_status otb_dyn_session_step(otb_dyn_session* ss, const double* props, double* state_out,
+                                           void* stream) {
+  if (!ss || !props || !state_out) return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  if (ss->k >= ss->num_steps) return set_error(OTB_ERR_INVALID_ARG, "the process tensor has no further step");
+  otb_pt* h = ss->pt;
+  const PtDev& I = h->inst[ss->inst];
+  const int D = I.D, nh = ss->nh, k = ss->k;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!check_cuda(cudaMemcpyAsync(ss->dtab.p, props, (size_t)nh * 2 * D * D * 16, cudaMemcpyHostToDevice, s),
+                  "upload"))
+    return OTB_ERR_CUDA;
+  DynLaunch L{};
+  L.nh = nh;
+  L.D = D;
+  L.d = I.d;
+  L.sites = (const double*)h->d_sites.p + 2 * I.site_base;
+  L.slot_elems = (long long)I.cap * D * I.cap;
+  L.dims = (const int2*)h->d_dims.p + I.dims_base;
+  L.caps = (const double*)h->d_caps.p + 2 * I.caps_base;
+  L.cap = I.cap;
+  L.ptab = (const double*)ss->dtab.p;
+  L.pidx = (const int*)ss->didx.p;
+  L.pidx_stride = ss->num_steps;
+  L.vcur = (k % 2 == 0) ? (double*)ss->dv0.p : (double*)ss->dv1.p;
+  L.vnext = (k % 2 == 0) ? (double*)ss->dv1.p : (double*)ss->dv0.p;
+  L.out = (double*)ss->dout.p;
+  L.partial = (double*)ss->dpart.p;
+  L.counter = (unsigned int*)ss->dcnt.p;
+  L.max_chunks = (I.cap + 31) / 32;
+  L.k = k;
+  if (!check_cuda(launch_dyn_step(L, ss->dims[k].y, s), "dyn step")) return OTB_ERR_CUDA;
+  const size_t sb = (size_t)nh * D * 16;
+  if (!check_cuda(cudaMemcpyAsync(state_out, (char*)ss->dout.p + (size_t)(k + 1) * sb, sb,
+                                  cudaMemcpyDeviceToHost, s),
+                  "download") ||
+      !check_cuda(cudaStreamSynchronize(s), "sync"))
+    return OTB_ERR_CUDA;
+  ss->k = k + 1;
+  return OTB_OK;
+}
+
+extern "C" otb_status otb_dyn_session_state(otb_dyn_session* ss, int32_t step, double* state_out) {
+  if (!ss || !state_out || step < 0 || step > ss->k) return set_error(OTB_ERR_INVALID_ARG, "bad arguments");
+  const size_t sb = (size_t)ss->nh * ss->pt->inst[ss->inst].D * 16;
+  if (!check_cuda(cudaMemcpy(state_out, (char*)ss->dout.p + (size_t)step * sb, sb, cudaMemcpyDeviceToHost),
+                  "download"))
+    return OTB_ERR_CUDA;
+  return OTB_OK;
+}
+
+extern "C" void otb_dyn_session_destroy(otb_dyn_session* ss) { delete ss; }
+
 extern "C" otb_status otb_dyn_gradient(otb_pt* h, int32_t inst, int32_t nh, const double* props,
                                        int32_t n_props, const int32_t* prop_index, const double* rho0,
                                        const double* target, int32_t num_steps, double* out_states,

@@ -29,7 +29,9 @@ first copied to a host ``SimpleProcessTensor``).  Both
 ``compute_correlations_nt`` (which ``compute_correlations`` calls): on a
 device process tensor its runs become the slots of one batched sweep; and
 ``oqupy.gradient.compute_gradient_and_dynamics`` (which ``state_gradient``
-calls), whose forward and adjoint sweeps run on the GPU.
+calls), whose forward and adjoint sweeps run on the GPU; and
+``compute_dynamics_with_field`` (mean-field dynamics on process tensors),
+whose sweeps advance on the GPU one step per host field update.
 """
 
 from typing import Any, Dict, Optional
@@ -291,6 +293,67 @@ def install(oqupy_module: Any = None) -> None:
         compute_gradient_and_dynamics.reference_function = ref_grad
         grad_mod.compute_gradient_and_dynamics = compute_gradient_and_dynamics
 
+        # compute_dynamics_with_field (system_dynamics.py:184-476): mean-field
+        # dynamics on device process tensors, one sweep step per call
+        ref_wf = sd_mod.compute_dynamics_with_field
+        _installed["compute_dynamics_with_field"] = ref_wf
+        _installed["compute_dynamics_with_field_pkg"] = getattr(oqupy_module, "compute_dynamics_with_field", None)
+
+        def single_device_pt(p):
+            if isinstance(p, list):
+                return p[0] if len(p) == 1 and isinstance(p[0], dev_cls) else None
+            return p if isinstance(p, dev_cls) else None
+
+        def compute_dynamics_with_field(mean_field_system, initial_field, process_tensor_list=None,
+                                        dt=None, num_steps=None, initial_state_list=None,
+                                        start_time=0.0, control_list=None, record_all=True,
+                                        subdiv_limit=sd_mod.SUBDIV_LIMIT,
+                                        liouvillian_epsrel=sd_mod.INTEGRATE_EPSREL, progress_type=None):
+            kwargs = dict(process_tensor_list=process_tensor_list, dt=dt, num_steps=num_steps,
+                          initial_state_list=initial_state_list, start_time=start_time,
+                          control_list=control_list, record_all=record_all, subdiv_limit=subdiv_limit,
+                          liouvillian_epsrel=liouvillian_epsrel, progress_type=progress_type)
+            devs = [single_device_pt(p) for p in (process_tensor_list or [])]
+            n_sys = len(mean_field_system.system_list)
+            if not (record_all and len(devs) == n_sys and all(d is not None for d in devs)):
+                if process_tensor_list is not None:
+                    kwargs["process_tensor_list"] = [
+                        [host_copy(q) for q in p] if isinstance(p, list) else host_copy(p)
+                        for p in process_tensor_list]
+                return ref_wf(mean_field_system, initial_field, **kwargs)
+            states0 = initial_state_list if initial_state_list is not None else [None] * n_sys
+            controls_in = control_list if control_list is not None else [None] * n_sys
+            parsed = [sd_mod._compute_dynamics_input_parse(True, system, st, dt, num_steps, start_time,
+                                                           pt, ctl, record_all)
+                      for system, st, pt, ctl in zip(mean_field_system.system_list, states0,
+                                                     process_tensor_list, controls_in)]
+            num_steps_, dt_ = parsed[0][3], parsed[0][2]
+            props = [system.get_propagators(dt_, start_time, subdiv_limit, liouvillian_epsrel)
+                     for system in mean_field_system.system_list]
+            ctls = []
+            for ctl in controls_in:
+                if ctl is None:
+                    ctls.append(None)
+                    continue
+                c = {"pre": {}, "post": {}}
+                for step in range(num_steps_ + 1):
+                    pre, post = ctl.get_controls(step, dt=dt_, start_time=start_time)
+                    if pre is not None:
+                        c["pre"][step] = pre
+                    if post is not None:
+                        c["post"][step] = post
+                ctls.append(c)
+            from .mean_field import device_dynamics_with_field
+            times, states, fields = device_dynamics_with_field(
+                props, mean_field_system.field_eom, initial_field, devs,
+                [p[1].reshape(-1) for p in parsed], num_steps_, dt_, start_time, ctls)
+            return dyn_mod.MeanFieldDynamics(times=times, system_states_list=states, fields=fields)
+
+        compute_dynamics_with_field.reference_function = ref_wf
+        sd_mod.compute_dynamics_with_field = compute_dynamics_with_field
+        if _installed["compute_dynamics_with_field_pkg"] is not None:
+            oqupy_module.compute_dynamics_with_field = compute_dynamics_with_field
+
 
 def uninstall(oqupy_module: Any = None) -> None:
     if oqupy_module is None:
@@ -315,6 +378,10 @@ def uninstall(oqupy_module: Any = None) -> None:
         sd_mod.compute_correlations_nt = _installed.pop("compute_correlations_nt")
         grad_mod = importlib.import_module(oqupy_module.__name__ + ".gradient")
         grad_mod.compute_gradient_and_dynamics = _installed.pop("compute_gradient_and_dynamics")
+        sd_mod.compute_dynamics_with_field = _installed.pop("compute_dynamics_with_field")
+        pkg = _installed.pop("compute_dynamics_with_field_pkg", None)
+        if pkg is not None:
+            oqupy_module.compute_dynamics_with_field = pkg
         pkg = _installed.pop("compute_correlations_nt_pkg", None)
         if pkg is not None:
             oqupy_module.compute_correlations_nt = pkg

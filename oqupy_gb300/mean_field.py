@@ -9,6 +9,11 @@ each system's propagators from the current states and field (the user's
 callables), uploads the propagators of all systems in one copy, advances the
 batch, reads the next states back and evaluates the next field
 (tempo_backend.py:747-773).
+
+``device_dynamics_with_field`` is the process-tensor form
+(``compute_dynamics_with_field``, system_dynamics.py:184-476): the systems'
+sweeps over their device process tensors advance one step per call, with
+the field evaluated on the host in between.
 """
 
 from copy import deepcopy
@@ -172,3 +177,95 @@ class GpuMeanFieldTempoBackend:
         if self._batch is not None:
             self._batch.close()
             self._batch = None
+
+
+def device_dynamics_with_field(propagators_list, field_eom, initial_field, process_tensors,
+                               initial_states, num_steps: int, dt: float, start_time: float = 0.0,
+                               controls=None):
+    """``compute_dynamics_with_field`` (system_dynamics.py:184-476) with one
+    device process tensor per system: every step reads the systems' states,
+    advances the field by the reference's second-order Runge-Kutta rule,
+    evaluates each system's propagators from the field and its derivative
+    and advances all systems that share a process tensor in one sweep step
+    (``otb_dyn_session_step``).
+
+    ``propagators_list[i](step, field, field_derivative) -> (P1, P2)``;
+    ``field_eom(t, states, field)`` with ``d x d`` states;
+    ``process_tensors[i]``: a ``DeviceProcessTensor`` (or ``(PtBatch, i)``);
+    ``controls[i]``: ``None`` or ``{"pre": {step: C}, "post": {step: C}}``.
+    Returns ``(times, states[num_steps+1][system] (d x d), fields)``."""
+    from .correlations import _pt_handle
+    n_sys = len(propagators_list)
+    controls = [None] * n_sys if controls is None else list(controls)
+    D = [np.asarray(s).size for s in initial_states]
+    dims = [int(round(np.sqrt(x))) for x in D]
+    # systems that share a process tensor share one session
+    groups = {}
+    for i, pt in enumerate(process_tensors):
+        groups.setdefault(id(pt), []).append(i)
+    sessions = []
+    for key, members in groups.items():
+        batch, idx, tin, tout = _pt_handle(process_tensors[members[0]])
+        rho0 = []
+        for i in members:
+            r = np.asarray(initial_states[i], dtype=np.complex128).reshape(-1)
+            pre0 = (controls[i] or {}).get("pre", {}).get(0)
+            rho0.append(r if pre0 is None else np.asarray(pre0) @ r)
+        sessions.append((members, batch.session(idx, np.array(rho0)), tin, tout))
+
+    def mats(vecs):
+        return [np.asarray(v).reshape(d, d) for v, d in zip(vecs, dims)]
+
+    def rk2(t, prev, field, cur):
+        rk1 = field_eom(t, mats(prev), field)
+        rk2_ = field_eom(t + dt, mats(cur), field + rk1 * dt)
+        return field + dt * (rk1 + rk2_) / 2
+
+    current = [None] * n_sys
+    for members, sess, _, _ in sessions:
+        st = sess.state(0)
+        for j, i in enumerate(members):
+            current[i] = st[j]
+    states, fields = [], []
+    field = complex(initial_field)
+    previous = None
+    try:
+        for step in range(num_steps):
+            t = start_time + step * dt
+            if step > 0:
+                field = rk2(t, previous, field, current)
+            previous = list(current)
+            states.append(mats(current))
+            fields.append(field)
+            deriv = field_eom(t, mats(current), field)
+            nxt = [None] * n_sys
+            for members, sess, tin, tout in sessions:
+                pairs = []
+                for i in members:
+                    p1, p2 = propagators_list[i](step, field, deriv)
+                    p1 = np.asarray(p1, dtype=np.complex128)
+                    p2 = np.asarray(p2, dtype=np.complex128)
+                    if tin is not None:
+                        p1 = np.asarray(tin).T @ p1
+                    if tout is not None:
+                        p2 = p2 @ np.asarray(tout).T
+                    ctl = controls[i] or {}
+                    post = ctl.get("post", {}).get(step)
+                    pre_next = ctl.get("pre", {}).get(step + 1)
+                    if post is not None:
+                        p1 = p1 @ np.asarray(post)
+                    if pre_next is not None:
+                        p2 = np.asarray(pre_next) @ p2
+                    pairs.append(np.stack([p1, p2]))
+                out = sess.step(np.array(pairs))
+                for j, i in enumerate(members):
+                    nxt[i] = out[j]
+            current = nxt
+        t = start_time + num_steps * dt
+        states.append(mats(current))
+        fields.append(rk2(t, previous, field, current) if num_steps > 0 else field)
+    finally:
+        for _, sess, _, _ in sessions:
+            sess.close()
+    times = start_time + np.arange(len(states)) * dt
+    return list(times), states, fields

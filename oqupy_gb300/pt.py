@@ -171,6 +171,11 @@ class PtBatch:
             nat.dptr(out), ctypes.c_void_p(stream or 0)))
         return out.view(np.complex128)[..., 0]
 
+    def session(self, i: int, rho0) -> "DynSession":
+        """A sweep over process tensor ``i`` advanced one step per call, for
+        ``H`` systems starting at ``rho0`` ``[H, D]``."""
+        return DynSession(self, i, rho0)
+
     def gradient_cores(self, i: int, props, prop_index, rho0, target, num_steps: int,
                        stream: Optional[int] = None):
         """Forward and adjoint sweeps of the gradient (``otb_dyn_gradient``)
@@ -191,6 +196,47 @@ class PtBatch:
             idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nat.dptr(nat.cplx(r0a)), nat.dptr(tg),
             n, nat.dptr(states), nat.dptr(cores), ctypes.c_void_p(stream or 0)))
         return states.view(np.complex128)[..., 0], cores.view(np.complex128)[..., 0]
+
+
+class DynSession:
+    """A process-tensor sweep advanced one step per call
+    (``otb_dyn_session_*``), for sweeps whose next propagators depend on the
+    states so far.  ``step(props)`` takes ``[H, 2, D, D]`` pairs (transforms
+    and controls folded in) and returns the ``[H, D]`` states after the
+    step."""
+
+    def __init__(self, batch: "PtBatch", i: int, rho0):
+        self.D = batch.meta[i]["D"]
+        r0 = np.asarray(rho0, dtype=np.complex128).reshape(-1, self.D)
+        self.n = r0.shape[0]
+        self._batch = batch          # the process tensor outlives the session
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().otb_dyn_session_create(batch._h, int(i), self.n, nat.dptr(nat.cplx(r0)),
+                                                   ctypes.byref(h)))
+        self._h = h
+
+    def step(self, props, stream: Optional[int] = None) -> np.ndarray:
+        tab = nat.cplx(np.asarray(props, dtype=np.complex128).reshape(self.n, 2, self.D, self.D))
+        out = np.zeros((self.n, self.D, 2))
+        nat.check(nat.lib().otb_dyn_session_step(self._h, nat.dptr(tab), nat.dptr(out),
+                                                 ctypes.c_void_p(stream or 0)))
+        return out.view(np.complex128)[..., 0]
+
+    def state(self, step: int) -> np.ndarray:
+        out = np.zeros((self.n, self.D, 2))
+        nat.check(nat.lib().otb_dyn_session_state(self._h, int(step), nat.dptr(out)))
+        return out.view(np.complex128)[..., 0]
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            nat.lib().otb_dyn_session_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class GpuPtTempoBackend:

@@ -24,6 +24,7 @@ Reference being restated (OQuPy 0.5.0, paths relative to the project root):
 * ``oqupy/backends/pt_tempo_backend.py:105-316`` ``PtTempoBackend``
 * ``oqupy/process_tensor.py:326-406``  ``get_mpo_tensor`` / ``compute_caps``
 * ``oqupy/system_dynamics.py:41-182, 631-700``  ``compute_dynamics``
+* ``oqupy/system_dynamics.py:184-476``  ``compute_dynamics_with_field``
 * ``oqupy/system_dynamics.py:791-990``  ``compute_correlations_nt``
 * ``oqupy/gradient.py:169-437``  ``compute_gradient_and_dynamics``
 * truncation rule of ``tensornetwork.split_node_full_svd(relative=True)``,
@@ -539,6 +540,64 @@ def compute_dynamics_pt(initial_state, propagators, mpo_tensors, caps,
         v = v @ np.asarray(p2, CDT).T
     states.append(np.einsum("ba,b->a", v, caps[num_steps]))
     return np.array(states)
+
+
+def dynamics_with_field_pt(initial_states, propagators_list, field_eom, initial_field,
+                           pts, num_steps, dt, start_time=0.0, controls_list=None):
+    """``compute_dynamics_with_field`` (system_dynamics.py:184-476) with one
+    process tensor per system: ``pts[i] = (mpo_tensors, caps, transform_in,
+    transform_out)``, ``propagators_list[i](step, field, derivative)``,
+    ``field_eom(t, states, field)`` on ``d x d`` states.  Per step: the
+    pre-measurement controls, the states, the field (initial value at step 0,
+    afterwards the second-order Runge-Kutta rule of :319-325 at time t from
+    the previous states), the post-measurement controls, the propagators from
+    the field and its derivative, one sweep step per system; at the end the
+    last states and one more field update.  Returns ``(states[num_steps+1]
+    [system], fields)``."""
+    n_sys = len(initial_states)
+    ctls = controls_list or [None] * n_sys
+    dims = [int(round(np.sqrt(np.asarray(s).size))) for s in initial_states]
+    vs = [np.asarray(s, dtype=CDT).reshape(1, -1) for s in initial_states]
+
+    def read(i, step):
+        return np.einsum("ba,b->a", vs[i], pts[i][1][step]).reshape(dims[i], dims[i])
+
+    def compute_field(t, prev, field, cur):
+        rk1 = field_eom(t, prev, field)
+        rk2 = field_eom(t + dt, cur, field + rk1 * dt)
+        return field + dt * (rk1 + rk2) / 2
+
+    states, fields = [], []
+    field = complex(initial_field)
+    prev = None
+    for step in range(num_steps + 1):
+        t = start_time + step * dt
+        for i in range(n_sys):
+            pre = ctls[i](step)[0] if ctls[i] is not None else None
+            if pre is not None:
+                vs[i] = vs[i] @ np.asarray(pre, CDT).T
+        if step == num_steps:
+            break
+        cur = [read(i, step) for i in range(n_sys)]
+        field = field if step == 0 else compute_field(t, prev, field, cur)
+        prev = cur
+        states.append(cur)
+        fields.append(field)
+        for i in range(n_sys):
+            post = ctls[i](step)[1] if ctls[i] is not None else None
+            if post is not None:
+                vs[i] = vs[i] @ np.asarray(post, CDT).T
+        deriv = field_eom(t, cur, field)
+        for i in range(n_sys):
+            p1, p2 = propagators_list[i](step, field, deriv)
+            mpos, caps, tin, tout = pts[i]
+            v = vs[i] @ np.asarray(p1, CDT).T
+            v = np.einsum("la,lrab->rb", v, pt_mpo_rank4(mpos[step], tin, tout))
+            vs[i] = v @ np.asarray(p2, CDT).T
+    final = [read(i, num_steps) for i in range(n_sys)]
+    states.append(final)
+    fields.append(compute_field(start_time + num_steps * dt, prev, field, final))
+    return states, fields
 
 
 def gradient_pt(initial_state, propagators, mpo_tensors, caps, num_steps, target,

@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 
 from tests import mean_field_cases as mfc  # noqa: E402
 
+sys.path.insert(0, HERE)
+from make_golden import _perturbed  # noqa: E402
+
 
 def _import_reference(ref_root):
     sys.path[:0] = [os.path.join(ROOT, "oracle", "tnshim"), ref_root]
@@ -108,6 +111,56 @@ def main(ref_root):
         out[f"{name}/field_envelope"] = fenv
         print(f"{name}: {n_sys} systems, {nsteps} steps, dkmax {dkmax}, final field {fields[-1]:.6f}, "
               f"envelope {env.max():.1e} (field {fenv.max():.1e})")
+    # the same models on process tensors: compute_dynamics_with_field
+    # (system_dynamics.py:184-476), one process tensor per system's bath
+    for name, case in mfc.CASES.items():
+        mft, baths, params = build(oqupy, case)
+        mfs = oqupy.MeanFieldSystem(
+            [oqupy.TimeDependentSystemWithField(
+                s["h"], gammas=[(lambda t, g=g: g) for g in s["gammas"]],
+                lindblad_operators=[(lambda t, a=a: a) for a in s["lops"]]) for s in case["systems"]],
+            field_eom=case["field_eom"])
+        end_time = case["nsteps"] * case["dt"]
+        pts = []
+        for i, bath in enumerate(baths):
+            ptt = oqupy.PtTempo(bath, 0.0, end_time, params)
+            pt = ptt.get_process_tensor(progress_type="silent")
+            pts.append(pt)
+            kmax = ptt._backend_instance._num_infl
+            out[f"{name}/pt_influences{i}"] = np.array([ptt._influence(dk) for dk in range(kmax)])
+            out[f"{name}/pt_dkmax{i}"] = np.int64(ptt._backend_instance._dkmax
+                                                   if ptt._backend_instance._dkmax is not None else -1)
+            if pt.transform_in is not None:
+                out[f"{name}/pt_transform_in{i}"] = np.asarray(pt.transform_in)
+                out[f"{name}/pt_transform_out{i}"] = np.asarray(pt.transform_out)
+        def run_pt(pts):
+            dyn = oqupy.compute_dynamics_with_field(
+                mfs, initial_field=case["field0"], process_tensor_list=pts,
+                initial_state_list=[np.asarray(s["rho0"]) for s in case["systems"]],
+                start_time=0.0, subdiv_limit=None, progress_type="silent")
+            st = np.array([[np.asarray(m).reshape(-1) for m in sd.states] for sd in dyn.system_dynamics])
+            return st, np.array(dyn.fields, dtype=np.complex128)
+        st, fl = run_pt(pts)
+        out[f"{name}/pt_states"] = st
+        out[f"{name}/pt_fields"] = fl
+        # spread: the process tensors rebuilt with influences perturbed by
+        # 1e-15 relative (two seeds)
+        env = np.zeros(st.shape[:2])
+        fenv = np.zeros(len(fl))
+        for seed in (1, 2):
+            pts2 = []
+            for bath in baths:
+                p2 = oqupy.PtTempo(bath, 0.0, end_time, params)
+                p2._backend_instance._influence = _perturbed(p2._backend_instance._influence, seed)
+                pts2.append(p2.get_process_tensor(progress_type="silent"))
+            st2, fl2 = run_pt(pts2)
+            for i in range(st.shape[0]):
+                env[i] = np.maximum(env[i], [trace_distance(a, b) for a, b in zip(st[i], st2[i])])
+            fenv = np.maximum(fenv, np.abs(fl - fl2))
+        out[f"{name}/pt_envelope"] = env
+        out[f"{name}/pt_field_envelope"] = fenv
+        print(f"{name} on process tensors: {st.shape[1] - 1} steps, final field {fl[-1]:.6f}, "
+              f"vs TEMPO {out[name + '/fields'][-1]:.6f}, envelope {env.max():.1e}")
     # the reference's own known answer for case G (default parameters)
     st, f, *_ = run(oqupy, mfc.CASES["dicke_G"], subdiv_limit="default")
     rho_g = np.array([[0.6245009 + 3.19373236e-15j, 0.14243496 - 2.19523032e-01j],

@@ -215,3 +215,161 @@ def test_mean_field_backend_host_logic(name, monkeypatch):
     for a, b in zip(states, ref_states):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(fields, ref_fields)
+
+
+# -- mean-field dynamics on process tensors (compute_dynamics_with_field) --
+
+def pt_inputs(g, name, i):
+    """(influence callable, dkmax, transforms) of system i's process tensor."""
+    infl = g[f"{name}/pt_influences{i}"]
+    dk = int(g[f"{name}/pt_dkmax{i}"])
+    dkmax = len(infl) - 1 if dk < 0 else dk       # full memory: every influence of the run
+    tin = g[f"{name}/pt_transform_in{i}"] if f"{name}/pt_transform_in{i}" in g.files else None
+    tout = g[f"{name}/pt_transform_out{i}"] if f"{name}/pt_transform_out{i}" in g.files else None
+    return (lambda k: infl[k] if k >= 0 else None), dkmax, tin, tout
+
+
+def oracle_pts(g, name):
+    case = mfc.CASES[name]
+    out = []
+    for i, s in enumerate(case["systems"]):
+        f, dkmax, tin, tout = pt_inputs(g, name, i)
+        d = int(round(np.sqrt(np.asarray(s["rho0"]).size)))
+        mpos, caps, _ = to.pt_tempo_build(d, f, case["nsteps"], dkmax, case["epsrel"])
+        out.append((mpos, caps, tin, tout))
+    return out
+
+
+def compare_pt(name, states, fields, g, abs_tol=1e-10):
+    ref = g[f"{name}/pt_states"]
+    env = g[f"{name}/pt_envelope"]
+    bad, worst = [], 0.0
+    for i in range(ref.shape[0]):
+        err = [to.trace_distance(np.asarray(a).reshape(-1), b) for a, b in zip([s[i] for s in states], ref[i])]
+        worst = max(worst, max(err))
+        bad += [("system", i) + v for v in gc.parity_violations(err, env[i], abs_tol)]
+    ferr = np.abs(np.asarray(fields) - g[f"{name}/pt_fields"])
+    fenv = np.maximum(g[f"{name}/pt_field_envelope"], env.max(axis=0))
+    bad += [("field",) + v for v in gc.parity_violations(ferr, fenv, abs_tol)]
+    return bad, worst, float(ferr.max())
+
+
+@pytest.mark.parametrize("name", sorted(mfc.CASES))
+def test_oracle_reproduces_reference_dynamics_with_field(name):
+    g = load()
+    case = mfc.CASES[name]
+    props = [mfc.propagators(s, case["dt"]) for s in case["systems"]]
+    states, fields = to.dynamics_with_field_pt([s["rho0"] for s in case["systems"]], props,
+                                               case["field_eom"], case["field0"], oracle_pts(g, name),
+                                               case["nsteps"], case["dt"])
+    bad, worst, fworst = compare_pt(name, states, fields, g)
+    print(name, f"{worst:.1e} {fworst:.1e}")
+    assert not bad, bad[:5]
+
+
+class SessionModelBatch:
+    """Stand-in for ``PtBatch.session``: the step of ``dyn_step_kernel``
+    (site storage ``[l][m][r]``, ``T = d * site``, one pair per system)
+    over the oracle's process tensor."""
+
+    def __init__(self, mpos, caps, d):
+        self.d = d
+        self.sites = [np.transpose(T, (0, 2, 1)) / d for T in mpos]
+        self.caps = caps
+
+    def session(self, i, rho0):
+        batch = self
+
+        class Session:
+            def __init__(self):
+                self.v = [np.asarray(r).reshape(1, -1) for r in np.asarray(rho0)]
+                self.k = 0
+
+            def state(self, step):
+                assert step == 0
+                return np.array([np.einsum("ra,r->a", v, batch.caps[0]) for v in self.v])
+
+            def step(self, props):
+                out = []
+                for h, (P1, P2) in enumerate(np.asarray(props)):
+                    u = np.einsum("ab,lb->la", P1, self.v[h])
+                    w = batch.d * np.einsum("la,lar->ra", u, batch.sites[self.k])
+                    self.v[h] = np.einsum("ab,rb->ra", P2, w)
+                    out.append(np.einsum("ra,r->a", self.v[h], batch.caps[self.k + 1]))
+                self.k += 1
+                return np.array(out)
+
+            def close(self):
+                pass
+        return Session()
+
+
+class FakeDevPt:
+    def __init__(self, batch, tin, tout):
+        self.device = (batch, 0)
+        self.transform_in, self.transform_out = tin, tout
+
+
+@pytest.mark.parametrize("name", sorted(mfc.CASES))
+def test_dynamics_with_field_host_logic_on_session_model(name):
+    from oqupy_gb300.mean_field import device_dynamics_with_field
+    g = load()
+    case = mfc.CASES[name]
+    pts = []
+    for (mpos, caps, tin, tout), s in zip(oracle_pts(g, name), case["systems"]):
+        d = int(round(np.sqrt(np.asarray(s["rho0"]).size)))
+        pts.append(FakeDevPt(SessionModelBatch(mpos, caps, d), tin, tout))
+    props = [mfc.propagators(s, case["dt"]) for s in case["systems"]]
+    times, states, fields = device_dynamics_with_field(
+        props, case["field_eom"], case["field0"], pts, [s["rho0"] for s in case["systems"]],
+        case["nsteps"], case["dt"])
+    assert len(times) == case["nsteps"] + 1
+    bad, worst, fworst = compare_pt(name, states, fields, g)
+    print(name, f"{worst:.1e} {fworst:.1e}")
+    assert not bad, bad[:5]
+
+
+def test_install_routes_dynamics_with_field(monkeypatch):
+    """``oqupy.compute_dynamics_with_field`` on a device process tensor goes
+    to ``mean_field.device_dynamics_with_field`` (here over the session
+    model) and returns the reference's numbers."""
+    from tests.reference_import import import_reference
+    oqupy = import_reference()
+    mfc.patch_field_hamiltonian_check(oqupy)
+    import oqupy_gb300
+    from oqupy_gb300 import mean_field
+    from oqupy_gb300.device_pt import device_process_tensor_class
+    g = load()
+    name = "dicke_G"
+    case = mfc.CASES[name]
+    s = case["systems"][0]
+    (mpos, caps, tin, tout), = oracle_pts(g, name)
+    batch = SessionModelBatch(mpos, caps, 2)
+    batch.meta = [dict(num_steps=len(mpos))]
+    batch.mpo_tensor = lambda i, k: np.array(mpos[k])
+    batch.cap = lambda i, k: np.array(caps[k])
+    batch.bond_dimensions = lambda i: np.array([m.shape[0] for m in mpos] + [mpos[-1].shape[1]])
+    batch.check_status = lambda: None
+    calls = []
+    real = mean_field.device_dynamics_with_field
+
+    def spy(*a, **k):
+        calls.append(1)
+        return real(*a, **k)
+    monkeypatch.setattr(mean_field, "device_dynamics_with_field", spy)
+    sysf = oqupy.TimeDependentSystemWithField(s["h"])
+    mfs = oqupy.MeanFieldSystem([sysf], field_eom=case["field_eom"])
+    oqupy_gb300.install(oqupy)
+    try:
+        cls = device_process_tensor_class(oqupy.process_tensor.BaseProcessTensor)
+        dev = cls(batch, 0, 2, case["dt"], tin, tout)
+        dyn = oqupy.compute_dynamics_with_field(mfs, initial_field=case["field0"],
+                                                process_tensor_list=[dev],
+                                                initial_state_list=[s["rho0"]], subdiv_limit=None,
+                                                progress_type="silent")
+    finally:
+        oqupy_gb300.uninstall(oqupy)
+    assert calls == [1]
+    states = [[np.asarray(m).reshape(-1)] for m in dyn.system_dynamics[0].states]
+    bad, worst, fworst = compare_pt(name, states, dyn.fields, g)
+    assert not bad, bad[:5]

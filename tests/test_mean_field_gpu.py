@@ -92,3 +92,73 @@ def test_mean_field_tempo_end_to_end():
     assert len(dyn.fields) == 21
     np.testing.assert_almost_equal(dyn.fields[-1], field_g, decimal=4)
     np.testing.assert_almost_equal(dyn.system_dynamics[0].states[-1], rho_g, decimal=4)
+
+
+@pytest.mark.parametrize("precision", ["complex128", "mixed"])
+@pytest.mark.parametrize("name", sorted(mfc.CASES))
+def test_gpu_dynamics_with_field_matches_reference(name, precision):
+    """compute_dynamics_with_field (system_dynamics.py:184-476) on process
+    tensors built on the device from the reference's influences."""
+    from oqupy_gb300.mean_field import device_dynamics_with_field
+    from oqupy_gb300.pt import PtBatch
+    from tests.test_mean_field_cpu import compare_pt, pt_inputs
+    g = load()
+    case = mfc.CASES[name]
+    pts, batches = [], []
+    for i, s in enumerate(case["systems"]):
+        f, dkmax, tin, tout = pt_inputs(g, name, i)
+        d = int(round(np.sqrt(np.asarray(s["rho0"]).size)))
+        b = PtBatch([dict(hs_dim=d, num_steps=case["nsteps"], dkmax=dkmax, epsrel=case["epsrel"],
+                          influences=g[f"{name}/pt_influences{i}"])],
+                    precision=precision, chi_cap=1152 // (d * d))
+        b.build()
+        batches.append(b)
+
+        class Pt:
+            device = (b, 0)
+            transform_in = tin
+            transform_out = tout
+        pts.append(Pt())
+    props = [mfc.propagators(s, case["dt"]) for s in case["systems"]]
+    times, states, fields = device_dynamics_with_field(
+        props, case["field_eom"], case["field0"], pts, [s["rho0"] for s in case["systems"]],
+        case["nsteps"], case["dt"])
+    for b in batches:
+        b.close()
+    tol = gc.PARITY_ABS if precision == "complex128" else gc.MIXED_ABS
+    bad, worst, fworst = compare_pt(name, states, fields, g, tol)
+    print(f"\n{name} {precision} on process tensors: max trace distance {worst:.2e}, "
+          f"max field error {fworst:.2e}")
+    assert not bad, bad[:5]
+
+
+def test_dynamics_with_field_end_to_end():
+    """The reference's tests/physics/mean_field_tempo_test.py case G on a
+    process tensor: pt_tempo_compute with the GPU backend, then
+    compute_dynamics_with_field routed to the device sweep."""
+    from tests.reference_import import import_reference
+    oqupy = import_reference()
+    mfc.patch_field_hamiltonian_check(oqupy)
+    import oqupy_gb300
+    case = mfc.CASES["dicke_G"]
+    s = case["systems"][0]
+    sysf = oqupy.TimeDependentSystemWithField(s["h"])
+    mfs = oqupy.MeanFieldSystem([sysf], field_eom=case["field_eom"])
+    corr = oqupy.PowerLawSD(alpha=s["alpha"], zeta=s["zeta"], cutoff=s["wc"],
+                            cutoff_type=s["cutoff_type"], temperature=s["T"])
+    bath = oqupy.Bath(s["coupling"], corr)
+    params = oqupy.TempoParameters(dt=case["dt"], tcut=case["tcut"], epsrel=case["epsrel"])
+    oqupy_gb300.install(oqupy)
+    try:
+        pt = oqupy.pt_tempo_compute(bath, start_time=0.0, end_time=1.0, parameters=params,
+                                    backend_config={"backend": "gb300"}, progress_type="silent")
+        dyn = oqupy.compute_dynamics_with_field(mfs, initial_field=case["field0"],
+                                                process_tensor_list=[pt],
+                                                initial_state_list=[s["rho0"]], progress_type="silent")
+    finally:
+        oqupy_gb300.uninstall(oqupy)
+    rho_g = np.array([[0.6245009 + 3.19373236e-15j, 0.14243496 - 2.19523032e-01j],
+                      [0.14243496 + 2.19523032e-01j, 0.3754991 - 2.26692588e-15j]])
+    field_g = 0.10602369935009 - 0.46986388684474406j
+    np.testing.assert_almost_equal(dyn.fields[-1], field_g, decimal=4)
+    np.testing.assert_almost_equal(dyn.system_dynamics[0].states[-1], rho_g, decimal=4)
