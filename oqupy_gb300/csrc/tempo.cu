@@ -21,13 +21,12 @@
 // is folded into the propagators on the host (P1 <- U_dag P1, P2 <- P2 U_sup),
 // so every influence here is in the coupling eigenbasis.
 //
-// Site tensors (complex128 in both precision forms) live in a per-instance
-// ring of fixed-capacity slots, layout [l][a][r] (row-major).  That layout is
-// also the column-major (a r) x l matrix the right-to-left sweep factorises,
-// so sweep splits need no reshuffle.  The precision forms differ in the bond
-// split (jacobi.cuh) and, in the mixed form, in the contractions (theta,
-// U / carry products, absorb), which run in double-float on the FP32 pipe
-// with their operands converted once per element (ff.cuh: ccacc_fma).
+// Site tensors live in a per-instance ring of fixed-capacity slots, layout
+// [l][a][r] (row-major), 16 bytes per element: complex128 in the complex128
+// form (tempo_step, below), double-float pairs in the mixed form
+// (tempo_step_ff, tempo_ff.cuh).  That layout is also the column-major
+// (a r) x l matrix the right-to-left sweep factorises, so sweep splits need
+// no reshuffle.
 #include <math.h>
 
 #include <climits>
@@ -86,7 +85,6 @@ __device__ __forceinline__ long long globaltimer_ns() {
   return (long long)t;
 }
 
-template <bool MIXED>
 __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R, int N, double epsrel, float qr_delta,
                      Bufs& b, SharedStep& sh, zc** Wout, bool* flip) {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -101,7 +99,7 @@ __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R,
   // QR workspace (16 bytes per element in both forms: cff or complex128)
   const bool qr = N >= QR_MIN_COLS;
   cff* Wff = nullptr;
-  if (MIXED || qr) {
+  if (qr) {
     Wff = (cff*)take((size_t)R * N * sizeof(cff));
     if (!Wff) Wff = b.Wffg;
   }
@@ -117,17 +115,10 @@ __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R,
   if (qr) {
     *flip = true;
     const size_t spare = (size_t)b.smem_bytes > used ? (size_t)b.smem_bytes - used : 0;
-    if (MIXED)
-      return qr_jacobi_truncate<ff>(W, R, N, Wff, b.smem + used, spare, epsrel, qr_delta, sh.norm, sh.perm,
-                                    &sh.jsh, Wout);
     return qr_jacobi_truncate<double>(W, R, N, reinterpret_cast<zc*>(Wff), b.smem + used, spare, epsrel,
                                       qr_delta, sh.norm, sh.perm, &sh.jsh, Wout);
   }
-  if (MIXED) {
-    kk = jacobi_truncate_mixed(W, R, N, Wff, epsrel, sh.norm, sh.perm, &sh.jsh);
-  } else {
-    kk = jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
-  }
+  kk = jacobi_truncate_fp64(W, R, N, R, epsrel, sh.norm, sh.perm, &sh.jsh);
   *Wout = W;
   return kk;
 }
@@ -138,7 +129,6 @@ __device__ __noinline__ int split(const zc* src, int lds, bool src_trans, int R,
 
 namespace otb {
 
-template <bool MIXED>
 __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& b,
                            SharedStep& sh) {
   const int tid = threadIdx.x;
@@ -220,16 +210,6 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     const int n = r * D;
     const zc* C = b.Cg;
     const bool last = (k == K - 1);
-    // mixed form: the contraction runs in double-float on the FP32 pipe, its
-    // operands converted once per element (carry -> Wffg, site -> Wg)
-    const bool ffc = MIXED && k > 0;
-    const cff* Cf = b.Wffg;
-    const cff* Af = reinterpret_cast<const cff*>(b.Wg);
-    if (ffc) {
-      for (int idx = tid; idx < cxd * ccd * D; idx += nt) b.Wffg[idx] = cff_from(C[idx]);
-      for (int idx = tid; idx < ccd * D * r; idx += nt) reinterpret_cast<cff*>(b.Wg)[idx] = cff_from(A[idx]);
-      __syncthreads();
-    }
     // theta into Tg: column-major (ld m) for a split, site layout for the last site
     for (int idx = tid; idx < m * n; idx += nt) {
       int row, col;
@@ -245,11 +225,6 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       zc acc = mk<double>(0, 0);
       if (k == 0) {
         acc = A[a * r + rr];
-      } else if (ffc) {
-        ccacc f = ccacc_zero();
-        for (int c = 0; c < ccd; ++c)
-          ccacc_fma(f, Cf[(long long)x * (ccd * D) + c * D + mr], Af[((long long)c * D + a) * r + rr]);
-        acc = ccacc_value(f);
       } else {
         for (int c = 0; c < ccd; ++c)
           cfma(acc, C[(long long)x * (ccd * D) + c * D + mr], A[((long long)c * D + a) * r + rr]);
@@ -266,14 +241,14 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     const bool trans = n > m;
     zc* W;
     bool flip;
-    const int kk = trans ? split<MIXED>(b.Tg, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
-                         : split<MIXED>(b.Tg, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
+    const int kk = trans ? split(b.Tg, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
+                         : split(b.Tg, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
     {
       const double R = trans ? n : m, N = trans ? m : n;
       flops += 8.0 * m * n * ccd + 4.0 * (6.0 * R * N * N + 20.0 * N * N * N);
     }
     ++splits;
-    sw64 += sh.jsh.sweeps;   // mixed form: FP64 fallback sweeps only
+    sw64 += sh.jsh.sweeps;
     sw32 += sh.jsh.sweeps32;
     if (sh.jsh.status != ST_OK || kk > cap) {
       if (tid == 0) sh.st.status = (sh.jsh.status != ST_OK) ? sh.jsh.status : ST_CHI_OVERFLOW;
@@ -282,51 +257,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
     }
     // W = theta V (U S) or W = theta^H U (V S), by orientation and driver
     const bool wt = flip ? !trans : trans;
-    if (MIXED && flip) {
-      // double-float products: theta -> Wg (the split's result lives in the
-      // Wff storage, so Wg is free), the kept columns of W -> Tg (theta's FP64
-      // copy is no longer read)
-      cff* Tf = reinterpret_cast<cff*>(b.Wg);
-      for (int idx = tid; idx < m * n; idx += nt) Tf[idx] = cff_from(b.Tg[idx]);
-      __syncthreads();
-      cff* Wf = reinterpret_cast<cff*>(b.Tg);
-      const int ldw = wt ? n : m;
-      for (int idx = tid; idx < kk * ldw; idx += nt) {
-        const int j = idx / ldw, q = idx - j * ldw;
-        Wf[idx] = cff_from(W[(long long)sh.perm[j] * ldw + q]);
-      }
-      __syncthreads();
-      if (!wt) {
-        // U = W[:, perm] / s -> site;  carry = U^H theta
-        for (int idx = tid; idx < m * kk; idx += nt) {
-          const int row = idx / kk, j = idx - row * kk;
-          const int pj = sh.perm[j];
-          A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
-        }
-        for (int idx = tid; idx < kk * n; idx += nt) {
-          const int j = idx / n, col = idx - j * n;
-          const cff* u = Wf + (long long)j * m;
-          const cff* th = Tf + (long long)col * m;
-          ccacc f = ccacc_zero();
-          for (int row = 0; row < m; ++row) ccacc_fmaj(f, u[row], th[row]);
-          b.Cg[idx] = cscale(ccacc_value(f), 1.0 / sh.norm[sh.perm[j]]);
-        }
-      } else {
-        // U = theta W[:, perm] / s^2 -> site;  carry = W[:, perm]^H
-        for (int idx = tid; idx < m * kk; idx += nt) {
-          const int row = idx / kk, j = idx - row * kk;
-          const double sj = sh.norm[sh.perm[j]];
-          const cff* w = Wf + (long long)j * n;
-          ccacc f = ccacc_zero();
-          for (int col = 0; col < n; ++col) ccacc_fma(f, Tf[(long long)col * m + row], w[col]);
-          A[idx] = cscale(ccacc_value(f), 1.0 / (sj * sj));
-        }
-        for (int idx = tid; idx < kk * n; idx += nt) {
-          const int j = idx / n, col = idx - j * n;
-          b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
-        }
-      }
-    } else if (!wt) {
+    if (!wt) {
       // U = W[:, perm] / s  -> site (cxd, D, kk);  carry = U^H theta
       for (int idx = tid; idx < m * kk; idx += nt) {
         const int row = idx / kk, j = idx - row * kk;
@@ -374,8 +305,8 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       const bool trans = n > m;
       zc* W;
       bool flip;
-      const int kk = trans ? split<MIXED>(A, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
-                           : split<MIXED>(A, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
+      const int kk = trans ? split(A, m, true, n, m, I.epsrel, I.qr_delta, b, sh, &W, &flip)
+                           : split(A, m, false, m, n, I.epsrel, I.qr_delta, b, sh, &W, &flip);
       {
         const double R = trans ? n : m, N = trans ? m : n;
         flops += 4.0 * (6.0 * R * N * N + 20.0 * N * N * N) + 8.0 * DIMS(k - 1).x * D * (double)kk * n;
@@ -389,50 +320,7 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
         break;
       }
       const bool wt = flip ? !trans : trans;
-      if (MIXED && flip) {
-        // double-float products; the site -> Wg, the kept columns of W -> Tg
-        // (first branch) or Cg (second branch, whose Tg holds the product)
-        cff* Af = reinterpret_cast<cff*>(b.Wg);
-        for (int idx = tid; idx < m * n; idx += nt) Af[idx] = cff_from(A[idx]);
-        const int ldw = wt ? n : m;
-        cff* Wf = reinterpret_cast<cff*>(wt ? b.Cg : b.Tg);
-        for (int idx = tid; idx < kk * ldw; idx += nt) {
-          const int j = idx / ldw, q = idx - j * ldw;
-          Wf[idx] = cff_from(W[(long long)sh.perm[j] * ldw + q]);
-        }
-        __syncthreads();
-        if (!wt) {
-          for (int idx = tid; idx < kk * n; idx += nt) {
-            const int j = idx / n, col = idx - j * n;
-            const cff* u = Wf + (long long)j * m;
-            const cff* y = Af + (long long)col * m;
-            ccacc f = ccacc_zero();
-            for (int row = 0; row < m; ++row) ccacc_fmaj(f, u[row], y[row]);
-            b.Cg[idx] = cscale(ccacc_value(f), 1.0 / sh.norm[sh.perm[j]]);
-          }
-          __syncthreads();
-          for (int idx = tid; idx < m * kk; idx += nt) {
-            const int j = idx / m, row = idx - j * m;
-            const int pj = sh.perm[j];
-            A[idx] = cscale(W[(long long)pj * m + row], 1.0 / sh.norm[pj]);
-          }
-        } else {
-          for (int idx = tid; idx < m * kk; idx += nt) {
-            const int j = idx / m, row = idx - j * m;
-            const double sj = sh.norm[sh.perm[j]];
-            const cff* w = Wf + (long long)j * n;
-            ccacc f = ccacc_zero();
-            for (int col = 0; col < n; ++col) ccacc_fma(f, Af[(long long)col * m + row], w[col]);
-            b.Tg[idx] = cscale(ccacc_value(f), 1.0 / (sj * sj));
-          }
-          __syncthreads();   // Wf (in Cg) is read above; the carry overwrites it
-          for (int idx = tid; idx < kk * n; idx += nt) {
-            const int j = idx / n, col = idx - j * n;
-            b.Cg[idx] = cconj(W[(long long)sh.perm[j] * n + col]);
-          }
-          for (int idx = tid; idx < m * kk; idx += nt) A[idx] = b.Tg[idx];
-        }
-      } else if (!wt) {
+      if (!wt) {
         for (int idx = tid; idx < kk * n; idx += nt) {
           const int j = idx / n, col = idx - j * n;
           const int pj = sh.perm[j];
@@ -470,29 +358,13 @@ __device__ void tempo_step(const TempoLaunch& L, const InstDev& I, int i, Bufs& 
       // absorb S V^H into site k-1: (l2, D, n) x (kk, n)^T -> (l2, D, kk)
       zc* B = SITE(k - 1);
       const int l2 = DIMS(k - 1).x;
-      if (MIXED) {
-        // double-float: site k-1 -> Wg, carry -> Wffg (the split's result is dead)
-        cff* Bf = reinterpret_cast<cff*>(b.Wg);
-        for (int idx = tid; idx < l2 * D * n; idx += nt) Bf[idx] = cff_from(B[idx]);
-        for (int idx = tid; idx < kk * n; idx += nt) b.Wffg[idx] = cff_from(b.Cg[idx]);
-        __syncthreads();
-        for (int idx = tid; idx < l2 * D * kk; idx += nt) {
-          const int la = idx / kk, j = idx - la * kk;
-          const cff* brow = Bf + (long long)la * n;
-          const cff* crow = b.Wffg + (long long)j * n;
-          ccacc f = ccacc_zero();
-          for (int c = 0; c < n; ++c) ccacc_fma(f, brow[c], crow[c]);
-          b.Tg[idx] = ccacc_value(f);
-        }
-      } else {
-        for (int idx = tid; idx < l2 * D * kk; idx += nt) {
-          const int la = idx / kk, j = idx - la * kk;
-          const zc* brow = B + (long long)la * n;
-          const zc* crow = b.Cg + (long long)j * n;
-          zc acc = mk<double>(0, 0);
-          for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
-          b.Tg[idx] = acc;
-        }
+      for (int idx = tid; idx < l2 * D * kk; idx += nt) {
+        const int la = idx / kk, j = idx - la * kk;
+        const zc* brow = B + (long long)la * n;
+        const zc* crow = b.Cg + (long long)j * n;
+        zc acc = mk<double>(0, 0);
+        for (int c = 0; c < n; ++c) cfma(acc, brow[c], crow[c]);
+        b.Tg[idx] = acc;
       }
       __syncthreads();
       for (int idx = tid; idx < l2 * D * kk; idx += nt) B[idx] = b.Tg[idx];
@@ -596,7 +468,7 @@ __global__ void __launch_bounds__(TEMPO_THREADS, 1) tempo_kernel(TempoLaunch L) 
       if (MIXED)
         tempo_step_ff(L, I, i, b, sh);
       else
-        tempo_step<false>(L, I, i, b, sh);
+        tempo_step(L, I, i, b, sh);
       __syncthreads();
       if (sh.st.status != ST_OK) break;
     }
@@ -752,7 +624,7 @@ __global__ void __launch_bounds__(STATIC_THREADS)
     if (MIXED)
       tempo_step_ff(L, I, 0, b, sh);
     else
-      tempo_step<false>(L, I, 0, b, sh);
+      tempo_step(L, I, 0, b, sh);
     __syncthreads();
     if (sh.st.status != ST_OK) break;
   }
