@@ -6,16 +6,19 @@ cutoff, H = Omega/2 sigma_x with Omega ~ U[0.5, 2], bath operator sigma_z/2,
 dkmax ~ U{20..300}, dt = 0.05, epsrel = 1e-6, 500 steps per trajectory,
 rho0 = spin up.  Inputs are synthetic (seeded draws of those distributions).
 
-One bench step = 25 TEMPO time steps of every instance (25 kernel launches),
-so ``--steps 20`` (the default) times whole 500-step trajectories and
-``value`` = whole trajectories per second of device time.  The headline form
-is "mixed" (pivoted QR + one-sided Jacobi and the contractions in
-double-float on the FP32 pipe; FP64 rank decisions and site storage); the
+One bench step = 25 TEMPO time steps of every instance (25 kernel launches;
+``--launch-steps m`` makes each launch run m steps), so ``--steps 20`` (the
+default) times whole 500-step trajectories and ``value`` = whole
+trajectories per second of device time.  The headline form is "mixed"
+(pivoted QR + one-sided Jacobi, the contractions and the site storage in
+double-float on the FP32 pipe; FP64 rank decisions); the
 complex128 form is timed on the first steps of the same instances, and the
 whole trajectories are compared with the FP64 oracle on a stratified
 subsample (committed fixture).  ``e2e`` is the same run through the host
 API, with every input uploaded and every state read back inside its timed
-region.
+region.  ``launch_timeline`` gives, per bench step, its last launch's
+per-instance device-clock spans (the longest instance against all
+instances' work spread over the SMs).
 
 ``--impl reference`` runs the reference's own CPU implementation (the
 unmodified OQuPy TempoBackend from baseline/_ref when it is importable, else
