@@ -18,7 +18,12 @@
  *                   (PtTempoBackend.__init__/initialize/compute_step/
  *                    get_mpo_tensor/update_process_tensor)
  *   otb_dyn_*    -> oqupy/system_dynamics.py:41-182, 631-700
- *                   (compute_dynamics hot loop over a process tensor)
+ *                   (compute_dynamics hot loop over a process tensor),
+ *                   with controls and time-dependent systems, the runs of
+ *                   compute_correlations_nt (:791-990), the sweep of
+ *                   compute_dynamics_with_field (:184-476) and the sweeps
+ *                   of compute_gradient_and_dynamics (gradient.py:169-437)
+ *   otb_mlp_*    -> no reference counterpart (learned screening surrogate)
  */
 #ifndef OQUPY_GB300_H
 #define OQUPY_GB300_H
